@@ -1,0 +1,372 @@
+#!/usr/bin/env python
+"""Fused-plan statevector benchmark on GB300.
+
+Workload (one "step"): the four fused circuits of the 30-qubit configuration,
+each from |0...0> on an 8 GiB complex64 state -- QAOA ring p=6, TFIM Trotter
+20 steps (J=1, h=0.7, dt=0.05), hardware-efficient ansatz depth 3, and random
+depth-10 U3 + CZ layers -- with seeded synthetic angles (qmetal_gb300/
+workloads.py). The metric is algorithmic HBM bytes per second: every plan op
+is charged 16 B per amplitude it must read and write (2S for dense, group,
+blocked and diagonal ops, S for controlled and swap ops, S/2 for CCX, S for
+the |0> reset, where S = 8 * 2^n bytes), over device time.
+
+Output: one JSON line (rank 0). `value` is device-timed with the state resident
+in HBM; `e2e` repeats the step through the C ABI from host gate arrays
+(circuit build, reset, run, 1024 samples and the norm read back), wall-clock;
+`roofline` is the dominant kernel's achieved bandwidth from CUDA events around
+each op inside the timed region; `cpu_baseline` is the complex128 oracle on
+the host cores on a bounded sample (the same circuits at 20 qubits).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Multi-GPU: the statevector path does not shard here; N GPUs run N independent
+replicas (weak scaling), one process per GPU under torchrun.
+"""
+from __future__ import annotations
+
+import argparse
+import concurrent.futures as cf
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_QUBITS = 30
+N_CPU = 20
+OP_NAMES = ["dense1q", "group", "blocked", "controlled1q", "diagonal", "swap", "ccx"]
+OP_STATE_PASSES = {0: 2.0, 1: 2.0, 2: 2.0, 3: 1.0, 4: 2.0, 5: 1.0, 6: 0.5}  # x S
+
+
+def workload(n):
+    from qmetal_gb300 import workloads as W
+    return [("qaoa_ring_p6", W.qaoa_ring_seeded(n, 6, seed=1)),
+            ("tfim_trotter_20", W.tfim_chain(n, 20, 1.0, 0.7, 0.05)),
+            ("hea_d3", W.hea(n, 3, seed=3)),
+            ("random_u3_d10", W.random_u3(n, 10, seed=4))]
+
+
+def plan_kinds(flat):
+    """Op kinds of a flat exported plan."""
+    out, pos = [], 1
+    for _ in range(int(flat[0])):
+        kind, ng, nt = int(flat[pos]), int(flat[pos + 5]), int(flat[pos + 6])
+        out.append(kind)
+        pos += 16 + 9 * ng + 2 * nt
+    return out
+
+
+def op_bytes(kind, n):
+    return OP_STATE_PASSES[kind] * 8.0 * (1 << n)
+
+
+def circuit_bytes(kinds, n):
+    """Reset (one state write) plus every plan op."""
+    return 8.0 * (1 << n) + sum(op_bytes(k, n) for k in kinds)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled during a region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device_index):
+        self.proc = None
+        self.device = device_index
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        self.lines = []
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out, _ = self.proc.communicate()
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in getattr(self, "lines", []):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx.append(float(f[2]))
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx),
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and "CUDA_VISIBLE_DEVICES" not in os.environ:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("gloo", init_method="env://")
+    return world, rank, local, dist
+
+
+def max_over_ranks(x, dist, world):
+    if world <= 1:
+        return x
+    import torch
+    t = torch.tensor([float(x)], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(dist, world):
+    if world > 1:
+        dist.barrier()
+
+
+def torch_sync():
+    try:
+        import torch
+        if torch.cuda.is_available():
+            torch.cuda.synchronize()
+    except Exception:
+        pass
+
+
+def cpu_oracle_run(n, gates):
+    import oracle
+    t0 = time.perf_counter()
+    oracle.run(n, gates)
+    return time.perf_counter() - t0
+
+
+def cpu_sample(threads, copies=1):
+    """The complex128 oracle (gate by gate, the reference's CPU algorithm) on
+    the workload's circuits at N_CPU qubits. Returns (GB/s-equivalent, secs)."""
+    import qmetal_gb300 as qm  # noqa: F401  (plan kinds come from the library)
+    from qmetal_gb300 import workloads as W
+    jobs, total_bytes = [], 0.0
+    for _name, gates in workload(N_CPU):
+        kinds = plan_kinds(W.to_circuit(N_CPU, gates).plan_export())
+        for _ in range(copies):
+            jobs.append(gates)
+            total_bytes += circuit_bytes(kinds, N_CPU)
+    t0 = time.perf_counter()
+    if threads == 1:
+        for g in jobs:
+            cpu_oracle_run(N_CPU, g)
+    else:
+        with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(lambda g: cpu_oracle_run(N_CPU, g), jobs))
+    dt = time.perf_counter() - t0
+    return total_bytes / dt / 1e9, dt
+
+
+def run_reference(args, world, rank, dist):
+    """The reference's CPU implementation of the path (the oracle port of its
+    complex128 Reference; its own sources are not on this machine), all host
+    threads, each step a bounded sample: every workload circuit at N_CPU
+    qubits, cores/4 copies of each run concurrently."""
+    if rank != 0:
+        return
+    import oracle
+    oracle.build()
+    threads = os.cpu_count() or 1
+    copies = max(1, threads // 4)
+    for _ in range(args.warmup):
+        cpu_sample(threads, copies)
+    rates, secs = [], 0.0
+    for _ in range(args.steps):
+        r, dt = cpu_sample(threads, copies)
+        rates.append(r)
+        secs += dt
+    value = args.steps / sum(1.0 / r for r in rates)   # total bytes / total time
+    kind = "reference" if oracle.ref_available() else "port"
+    line = {
+        "impl": "reference", "metric": "fused_plan_hbm_gbs", "value": round(value, 3),
+        "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
+        "config": {"workload": f"fused-plan circuits of the 30-qubit config, run at {N_CPU} "
+                               "qubits on the host (bounded sample)",
+                   "num_qubits": N_CPU, "circuits": [c for c, _ in workload(4)],
+                   "copies_per_circuit": copies},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
+                         "kind": kind,
+                         "sample": f"4 circuits x {copies} copies at n={N_CPU}, complex128, "
+                                   f"gate by gate, {threads} threads"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--qubits", type=int, default=N_QUBITS)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    world, rank, local, dist = dist_setup()
+    if args.impl == "reference":
+        run_reference(args, world, rank, dist)
+        barrier(dist, world)
+        return
+
+    import qmetal_gb300 as qm
+    from qmetal_gb300 import workloads as W
+    n = args.qubits
+    S = 8.0 * (1 << n)
+    circuits, kinds, gate_streams = [], [], []
+    for name, gates in workload(n):
+        c = W.to_circuit(n, gates)
+        circuits.append((name, c))
+        kinds.append(plan_kinds(c.plan_export()))
+        gate_streams.append(gates)
+    step_bytes = sum(circuit_bytes(k, n) for k in kinds)
+    sim = qm.Simulator(n)
+
+    def step():
+        for _name, c in circuits:
+            sim.reset()
+            sim.run(c)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    sim.synchronize()
+    torch_sync()
+    barrier(dist, world)
+
+    # --- device-timed region: per-op CUDA events on the simulator's stream ---
+    per_kind_time = {k: 0.0 for k in range(7)}
+    per_kind_count = {k: 0 for k in range(7)}
+    d0 = sim.dispatch_count
+    with ClockSampler(0 if world == 1 else local) as clocks:
+        sim.elapsed()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            for (name, c), ks in zip(circuits, kinds):
+                sim.reset()
+                secs = sim.run_profiled(c)
+                for k, s in zip(ks, secs):
+                    per_kind_time[k] += s
+                    per_kind_count[k] += 1
+        dev = sim.elapsed()
+        wall = time.perf_counter() - t0
+    launches = sim.dispatch_count - d0
+    torch_sync()
+    barrier(dist, world)
+    dev_max = max_over_ranks(dev, dist, world)
+    value = world * args.steps * step_bytes / dev_max / 1e9
+
+    # --- roofline of the dominant kernel ---------------------------------------
+    peak, peak_src = peaks()
+    dom = max(per_kind_time, key=lambda k: per_kind_time[k])
+    dom_bytes = per_kind_count[dom] * op_bytes(dom, n)
+    achieved = dom_bytes / per_kind_time[dom] / 1e9 if per_kind_time[dom] > 0 else 0.0
+    breakdown = {OP_NAMES[k]: {"ops": per_kind_count[k] // max(args.steps, 1),
+                               "ms_per_step": round(1e3 * per_kind_time[k] / args.steps, 3),
+                               "gbs": round(per_kind_count[k] * op_bytes(k, n) / per_kind_time[k] / 1e9, 1)
+                               if per_kind_time[k] > 0 else None}
+                 for k in range(7) if per_kind_count[k]}
+
+    # --- end to end through the C ABI, host gate arrays ----------------------
+    h2d = sum(sum(4 + 4 * len(q) + 8 * len(p) for _k, q, p in g) for g in gate_streams)
+    shots = 1024
+    d2h = len(circuits) * (shots * 8 + 8)
+    sim.synchronize()
+    torch_sync()
+    barrier(dist, world)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        for gates in gate_streams:
+            c = W.to_circuit(n, gates)
+            sim.reset()
+            sim.run(c)
+            sim.sample(shots, 7)
+            sim.norm()
+    sim.synchronize()
+    e2e_wall = max_over_ranks(time.perf_counter() - t0, dist, world)
+    e2e_value = world * args.steps * step_bytes / e2e_wall / 1e9
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        import oracle
+        oracle.build()
+        rate, secs = cpu_sample(1)
+        cpu = {"value": round(rate, 4), "unit": "GB/s", "cores": 1,
+               "kind": "reference" if oracle.ref_available() else "port",
+               "sample": f"the 4 circuits once at n={N_CPU}, complex128 gate by gate, "
+                         f"1 thread, {secs:.1f} s"}
+
+    if rank == 0:
+        ops_per_circuit = [len(k) for k in kinds]
+        line = {
+            "metric": "fused_plan_hbm_gbs", "value": round(value, 2), "unit": "GB/s",
+            "n_gpus": world, "steps": args.steps, "warmup": max(args.warmup, 3),
+            "ms_per_step": round(1e3 * dev_max / args.steps, 3),
+            "s_per_circuit": round(dev_max / args.steps / len(circuits), 5),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "c64", "data": "synthetic",
+            "config": {"workload": f"fused plans at n={n} from |0>: "
+                                   + ", ".join(c for c, _ in circuits),
+                       "num_qubits": n, "state_gib": S / 2 ** 30,
+                       "plan_ops": dict(zip([c for c, _ in circuits], ops_per_circuit)),
+                       "bytes_per_step": step_bytes,
+                       "l2": "inputs larger than L2 (state >> 129 MB), no flush",
+                       "parallelism": "replicas" if world > 1 else "single GPU"},
+            "roofline": {"bound": "hbm", "kernel": OP_NAMES[dom], "achieved": round(achieved, 1),
+                         "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
+                         "peak_source": peak_src,
+                         "traffic": None},
+            "kernels": breakdown,
+            "frac_of_peak_overall": round(value / world / peak, 4),
+            "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h},
+            "gpu_launches": int(launches),
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+            "wall_s_timed": round(wall, 3),
+        }
+        print(json.dumps(line), flush=True)
+    barrier(dist, world)
+
+
+if __name__ == "__main__":
+    main()

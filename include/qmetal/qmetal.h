@@ -1,0 +1,152 @@
+/* qmetal.h -- the stable C ABI of the qmetal statevector simulator, served by
+ * a CUDA executor on one NVIDIA GB300.
+ *
+ * Every declaration down to qm_energy_and_gradient is the reference project's
+ * ABI (include/qmetal/qmetal.h:14-113 there) with the same names, types,
+ * argument meanings, return conventions and gate numbering, so a caller built
+ * against the reference binds to this library unchanged. The declarations
+ * after it are appended extensions; nothing above them is renumbered.
+ *
+ * Conventions (unchanged):
+ *   - 0 on success, a negative code on failure; qm_last_error() holds the
+ *     calling thread's message. Nothing throws across the boundary.
+ *   - LSB-first: qubit q is bit q of the basis index.
+ *   - Amplitudes are complex64, interleaved (re, im, re, im, ...).
+ */
+#ifndef QMETAL_H
+#define QMETAL_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define QMETAL_VERSION_MAJOR 0
+#define QMETAL_VERSION_MINOR 1
+#define QMETAL_VERSION_PATCH 0
+
+/* Gate codes; ABI, append only (reference qmetal.h:28-36). */
+typedef enum {
+  QM_X = 0, QM_Y = 1, QM_Z = 2, QM_H = 3,
+  QM_S = 4, QM_SDG = 5, QM_T = 6, QM_TDG = 7,
+  QM_RX = 8, QM_RY = 9, QM_RZ = 10, QM_P = 11,
+  QM_CX = 12, QM_CY = 13, QM_CZ = 14, QM_SWAP = 15,
+  QM_CP = 16,
+  QM_CCX = 17
+} qm_gate_kind;
+
+typedef struct qm_simulator_s *qm_simulator;
+typedef struct qm_circuit_s *qm_circuit;
+
+/* A Hamiltonian as parallel arrays: one coefficient and three Pauli masks per
+ * term; borrowed for the duration of a call (reference qmetal.h:41-50). */
+typedef struct {
+  uint32_t num_terms;
+  const double *coeffs;
+  const uint64_t *x_masks;
+  const uint64_t *y_masks;
+  const uint64_t *z_masks;
+} qm_hamiltonian;
+
+/* --- diagnostics (reference qmetal.h:54-60; src/capi.cpp:92-124) --------- */
+void qm_version(int *major, int *minor, int *patch);
+const char *qm_last_error(void);          /* thread-local */
+int qm_is_available(void);                /* 1 if a CUDA device is usable */
+const char *qm_device_name(void);
+uint64_t qm_max_buffer_length(void);      /* largest state buffer, bytes */
+uint64_t qm_recommended_working_set(void);/* device memory, bytes */
+uint32_t qm_max_qubits(void);             /* 34 on this build */
+
+/* --- circuits (reference qmetal.h:64-73; src/capi.cpp:128-171) ----------- */
+qm_circuit qm_circuit_create(uint32_t num_qubits);
+void qm_circuit_destroy(qm_circuit c);
+int qm_circuit_add(qm_circuit c, qm_gate_kind kind, const uint32_t *qubits,
+                   uint32_t num_qubits, const double *params,
+                   uint32_t num_params);
+size_t qm_circuit_size(qm_circuit c);
+/* GPU passes the circuit lowers to: fuse = 0 gives the gate count. */
+size_t qm_circuit_plan_size(qm_circuit c, int fuse);
+
+/* --- simulator (reference qmetal.h:77-107; src/capi.cpp:175-274) --------- */
+qm_simulator qm_create(uint32_t num_qubits);
+void qm_destroy(qm_simulator s);
+
+int qm_reset(qm_simulator s);
+int qm_run(qm_simulator s, qm_circuit c);         /* fused, default passes */
+int qm_run_unfused(qm_simulator s, qm_circuit c); /* one op per gate */
+int qm_synchronize(qm_simulator s);
+
+uint32_t qm_num_qubits(qm_simulator s);
+uint64_t qm_dim(qm_simulator s);
+uint64_t qm_dispatch_count(qm_simulator s);       /* kernels launched */
+
+/* View of the interleaved state, 2 * qm_dim() floats, valid until the next
+ * mutation. Here the state lives in device memory; the returned pointer is a
+ * host mirror refreshed by this call. NULL on error. */
+const float *qm_amplitudes(qm_simulator s);
+
+int qm_norm(qm_simulator s, double *out);
+int qm_expectation_pauli(qm_simulator s, uint64_t x_mask, uint64_t y_mask,
+                         uint64_t z_mask, double *out);
+int qm_expectation(qm_simulator s, const qm_hamiltonian *h, double *out);
+
+/* `shots` basis indices without collapsing the state; splitmix64 stream, so
+ * identical seeds give identical samples. */
+int qm_sample(qm_simulator s, size_t shots, uint64_t seed, uint64_t *out);
+
+/* Adjoint gradient: `out_grad` holds qm_circuit_size(c) entries, 0 for gates
+ * without a parameter. Fails if a parameterised gate is not RX, RY or RZ. */
+int qm_energy_and_gradient(qm_simulator s, qm_circuit c,
+                           const qm_hamiltonian *h, double *out_energy,
+                           double *out_grad);
+
+/* ======================= appended extensions ============================= */
+/* None of these has a counterpart in the reference ABI. */
+
+/* Load / read the whole state (2 * count floats, count == qm_dim(s)). */
+int qm_set_state(qm_simulator s, const float *interleaved, uint64_t count);
+int qm_get_state(qm_simulator s, float *interleaved, uint64_t count);
+
+/* Apply one gate with no plan in between (the reference's C++
+ * Simulator::apply(const Gate&), src/metal/simulator.mm:348-434). */
+int qm_apply_gate(qm_simulator s, qm_gate_kind kind, const uint32_t *qubits,
+                  uint32_t num_qubits, const double *params,
+                  uint32_t num_params);
+
+/* Run with explicit fusion options (FusionOptions, reference plan.h:76-94). */
+int qm_run_options(qm_simulator s, qm_circuit c, int collapse_1q_windows,
+                   int fuse_diagonals, int recognize_zz, uint32_t group_1q,
+                   uint32_t block_bits);
+
+/* The plan the options produce, in a flat double layout:
+ *   [num_ops] then per op: kind, q0, q1, q2, block_bits, n_group, n_terms,
+ *   global_phase, matrix[8], group_qubits[n_group],
+ *   group_matrices[8 * n_group], masks[n_terms], angles[n_terms].
+ * Writes at most `cap` doubles; returns the full length, or 0 on error. */
+size_t qm_circuit_plan_export(qm_circuit c, int collapse_1q_windows,
+                              int fuse_diagonals, int recognize_zz,
+                              uint32_t group_1q, uint32_t block_bits,
+                              double *out, size_t cap);
+
+/* Per-term expectation values <P_t> (without the coefficients), one entry
+ * per Hamiltonian term, computed in grouped passes over the state. */
+int qm_expectation_terms(qm_simulator s, const qm_hamiltonian *h,
+                         double *out_values);
+
+/* Device-side timing of everything queued since the last call, in seconds
+ * (CUDA events on the simulator's stream). Synchronizes. */
+int qm_elapsed(qm_simulator s, double *out_seconds);
+
+/* Run the circuit's plan (fuse != 0: default fusion; 0: one op per gate) with
+ * a CUDA event between consecutive ops, then report each op's device time in
+ * seconds (at most `cap` entries) and the op count. Synchronizes. */
+int qm_run_profiled(qm_simulator s, qm_circuit c, int fuse, double *out_seconds,
+                    size_t cap, size_t *out_count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMETAL_H */

@@ -1,0 +1,132 @@
+/* qmetal_kernels.h -- the thin C-ABI layer between the C++ host and the
+ * hand-written sm_103a kernels.
+ *
+ * Plain device pointers and sizes only; a CUDA stream travels as void*
+ * (cudaStream_t). Every state pointer addresses 2^n complex64 amplitudes,
+ * interleaved (re, im), LSB-first, 16-byte aligned. Matrices are row-major
+ * 2x2 complex as 8 floats (re00, im00, re01, im01, re10, im10, re11, im11).
+ * Every entry point returns 0 on success, a positive cudaError_t value when a
+ * launch fails, or -1 for arguments it rejects (nothing is launched then).
+ *
+ * Each function names the reference kernel it replaces (file:line in the
+ * reference project's src/metal/kernels.metal, and the host code that drove
+ * it in src/metal/simulator.mm).
+ */
+#ifndef QMETAL_KERNELS_H
+#define QMETAL_KERNELS_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* |0...0>. Replaces init_basis (kernels.metal:39-44; simulator.mm:340-346). */
+int qmk_init_basis(float *state, uint32_t n, void *stream);
+
+/* 2x2 on wire q. Replaces apply_1q (kernels.metal:48-61; simulator.mm:453-463). */
+int qmk_apply_1q(float *state, uint32_t n, uint32_t q, const float m[8],
+                 void *stream);
+
+/* Multiply every amplitude whose index has all `mask` bits set by
+ * (re + i im); mask has 1..3 bits. Replaces apply_diagonal_2q
+ * (kernels.metal:168-178; simulator.mm:388-402), and serves diag(1, e^{ia})
+ * one-qubit gates at a quarter of the traffic of a dense 2x2. */
+int qmk_apply_phase(float *state, uint32_t n, uint64_t mask, float re,
+                    float im, void *stream);
+
+/* k in 2..5 commuting 2x2s on distinct ascending wires, one pass, amplitudes
+ * held in registers. Replaces apply_1q_group{2,3,4} (kernels.metal:71-102;
+ * simulator.mm:500-525). */
+int qmk_apply_group(float *state, uint32_t n, uint32_t k,
+                    const uint32_t *qubits, const float *matrices,
+                    void *stream);
+
+/* A run of `count` 2x2s on wires < block_bits applied in order to each
+ * 2^block_bits block staged in shared memory; block_bits in 2..14.
+ * Replaces apply_1q_blocked (kernels.metal:112-143; simulator.mm:464-499). */
+int qmk_apply_blocked(float *state, uint32_t n, uint32_t block_bits,
+                      uint32_t count, const uint32_t *qubits,
+                      const float *matrices, void *stream);
+
+/* 2x2 on `target` where every control bit is set; 1 or 2 controls (CX, CY,
+ * CCX). Replaces apply_controlled_1q (kernels.metal:148-163;
+ * simulator.mm:526-537) and apply_ccx (kernels.metal:392-408). */
+int qmk_apply_controlled(float *state, uint32_t n, uint32_t num_controls,
+                         const uint32_t *controls, uint32_t target,
+                         const float m[8], void *stream);
+
+/* Exchange |..1_a..0_b..> and |..0_a..1_b..>. Replaces apply_swap
+ * (kernels.metal:181-194; simulator.mm:538-547). */
+int qmk_apply_swap(float *state, uint32_t n, uint32_t a, uint32_t b,
+                   void *stream);
+
+/* Scratch bytes every workspace must hold for a simulator of n qubits (the
+ * diagonal-layer tables and reduction partials). */
+size_t qmk_workspace_bytes(uint32_t n);
+
+/* Zero the workspace bookkeeping (call once after allocating it). */
+int qmk_workspace_init(void *workspace, size_t bytes, void *stream);
+
+/* amplitude i *= exp(i (global_phase + sum of angles[t] over terms whose mask
+ * is fully set in i)), one pass. Phase sums are formed in FP64.
+ * Replaces apply_diagonal_layer (kernels.metal:203-218; simulator.mm:559-592). */
+int qmk_apply_diagonal(float *state, uint32_t n, uint32_t num_terms,
+                       const uint64_t *masks, const double *angles,
+                       double global_phase, void *workspace,
+                       size_t workspace_bytes, void *stream);
+
+/* sum |a_i|^2 into *d_out (device double). FP32 per-thread runs, FP64 from
+ * the warp up, fixed-order final sum. Replaces reduce_abs2
+ * (kernels.metal:250-268; simulator.mm:615-625). */
+int qmk_abs2sum(const float *state, uint32_t n, double *d_out,
+                void *workspace, size_t workspace_bytes, void *stream);
+
+/* Terms sharing one flip mask (flip = x|y), up to 16 per call. d_out[t]
+ * receives <psi|P_t|psi> for sign mask sign_masks[t] (= y|z) and Y count
+ * ny[t]. Replaces reduce_pauli (kernels.metal:273-307; simulator.mm:629-661). */
+int qmk_pauli_expect(const float *state, uint32_t n, uint64_t flip,
+                     uint32_t num_terms, const uint64_t *sign_masks,
+                     const uint32_t *ny, double *d_out, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+/* lambda (=|+=) sum_t coeff_t * i^ny_t * P_t psi over terms sharing one flip
+ * mask, up to 16 per call; coeffs real. overwrite != 0 stores instead of
+ * accumulating. Replaces pauli_accum + zero_state (kernels.metal:313-327,
+ * 363-367; simulator.mm:856-895). */
+int qmk_pauli_accum(float *lambda, const float *psi, uint32_t n,
+                    uint64_t flip, uint32_t num_terms,
+                    const uint64_t *sign_masks, const uint32_t *ny,
+                    const double *coeffs, int overwrite, void *stream);
+
+/* Re<a|b> into *d_out. Replaces the host energy loop of simulator.mm:897-904. */
+int qmk_dot_re(const float *a, const float *b, uint32_t n, double *d_out,
+               void *workspace, size_t workspace_bytes, void *stream);
+
+/* One backward step of the adjoint sweep for a one-qubit gate on wire q:
+ * if generator is 1/2/3 (X/Y/Z), *d_grad = Im<lambda|P_q|psi> taken before
+ * the undo; then minv (the gate's inverse) is applied to both psi and
+ * lambda, in the same pass. generator 0 only undoes. Replaces reduce_pauli2
+ * plus the two undo dispatches (kernels.metal:331-360; simulator.mm:914-959). */
+int qmk_adjoint_1q(float *psi, float *lambda, uint32_t n, uint32_t q,
+                   const float minv[8], int generator, double *d_grad,
+                   void *workspace, size_t workspace_bytes, void *stream);
+
+/* Sampling workspace bytes for n qubits (block CDF in FP64). */
+size_t qmk_sample_workspace_bytes(uint32_t n);
+
+/* Draw `shots` basis indices into d_out (device uint64) with the splitmix64
+ * stream of `seed`: FP64 block sums over 1024-amplitude blocks, device prefix
+ * scan, binary search per shot, warp walk inside the block. Replaces
+ * block_abs2 and the host CDF/search/walk (kernels.metal:372-387;
+ * simulator.mm:677-763). */
+int qmk_sample(const float *state, uint32_t n, uint64_t shots, uint64_t seed,
+               uint64_t *d_out, void *workspace, size_t workspace_bytes,
+               void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* QMETAL_KERNELS_H */

@@ -1,0 +1,450 @@
+// k_gates.cu -- in-place gate kernels: basis init, dense / controlled 2x2,
+// masked phase, register groups, shared-memory blocks, swap.
+//
+// Work is enumerated by "sites": the free vector-index bits left after the
+// op's own wires are taken out. A site expands to the one or more float4
+// vectors the op touches, so every thread moves whole 16-byte vectors and
+// consecutive threads move consecutive vectors. Each thread handles U sites
+// spaced kThreads apart (loads for all U first, then math, then stores) so
+// enough bytes are in flight to cover HBM latency.
+#include <algorithm>
+#include <cstring>
+#include <vector>
+
+#include "kcommon.cuh"
+#include "../../include/qmetal/qmetal_kernels.h"
+
+using namespace qmk;
+
+namespace {
+
+constexpr int U = 2;  // sites per thread
+
+__device__ __forceinline__ uint64_t site_of(int k) {
+  return (static_cast<uint64_t>(blockIdx.x) * U + k) * kThreads + threadIdx.x;
+}
+
+// Up to three ascending vector-bit positions to open, then forced-one bits.
+struct Fix {
+  uint32_t nfix;
+  uint32_t pos[3];
+  uint64_t set;
+};
+
+__device__ __forceinline__ uint64_t expand(uint64_t s, const Fix &f) {
+#pragma unroll
+  for (uint32_t j = 0; j < 3; j++)
+    if (j < f.nfix) s = ins0(s, f.pos[j]);
+  return s | f.set;
+}
+
+__global__ void k_init_basis(float4 *__restrict__ st, uint64_t nvec) {
+#pragma unroll
+  for (int k = 0; k < U; k++) {
+    const uint64_t v = site_of(k);
+    if (v < nvec) st[v] = make_float4(v == 0 ? 1.0f : 0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+// MODE 0: the target is amplitude bit 0, so the pair is the two lanes of one
+//         vector; controls (all >= 1) are forced-one vector bits.
+// MODE 1: target >= 1: the pair is vectors v and v|tbit, both lanes.
+// MODE 2: target >= 1 and amplitude bit 0 is a control: only the odd lane.
+template <int MODE>
+__global__ void __launch_bounds__(kThreads)
+k_pair(float4 *__restrict__ st, uint64_t nsites, Fix f, uint64_t tbit, M2 m) {
+  uint64_t v[U];
+  float4 A[U], B[U];
+#pragma unroll
+  for (int k = 0; k < U; k++) {
+    const uint64_t s = site_of(k);
+    v[k] = (s < nsites) ? expand(s, f) : ~0ull;
+    if (v[k] != ~0ull) {
+      A[k] = st[v[k]];
+      if (MODE != 0) B[k] = st[v[k] | tbit];
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < U; k++) {
+    if (v[k] == ~0ull) continue;
+    if (MODE == 0) {
+      float2 x = lo2(A[k]), y = hi2(A[k]);
+      apply2(m, x, y);
+      st[v[k]] = pack4(x, y);
+    } else if (MODE == 1) {
+      float2 a0 = lo2(A[k]), b0 = lo2(B[k]), a1 = hi2(A[k]), b1 = hi2(B[k]);
+      apply2(m, a0, b0);
+      apply2(m, a1, b1);
+      st[v[k]] = pack4(a0, a1);
+      st[v[k] | tbit] = pack4(b0, b1);
+    } else {
+      float2 a1 = hi2(A[k]), b1 = hi2(B[k]);
+      apply2(m, a1, b1);
+      float2 *s2 = reinterpret_cast<float2 *>(st);
+      s2[2 * v[k] + 1] = a1;
+      s2[2 * (v[k] | tbit) + 1] = b1;
+    }
+  }
+}
+
+// Multiply amplitudes with every mask bit set by `ph`. ODD: amplitude bit 0
+// is in the mask, so only the odd lane of each vector changes.
+template <bool ODD>
+__global__ void __launch_bounds__(kThreads)
+k_phase(float4 *__restrict__ st, uint64_t nsites, Fix f, float2 ph) {
+  if (ODD) {
+    float2 *s2 = reinterpret_cast<float2 *>(st);
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const uint64_t s = site_of(k);
+      if (s < nsites) {
+        const uint64_t i = 2 * expand(s, f) + 1;
+        s2[i] = cmul(ph, s2[i]);
+      }
+    }
+  } else {
+    uint64_t v[U];
+    float4 A[U];
+#pragma unroll
+    for (int k = 0; k < U; k++) {
+      const uint64_t s = site_of(k);
+      v[k] = (s < nsites) ? expand(s, f) : ~0ull;
+      if (v[k] != ~0ull) A[k] = st[v[k]];
+    }
+#pragma unroll
+    for (int k = 0; k < U; k++)
+      if (v[k] != ~0ull) st[v[k]] = pack4(cmul(ph, lo2(A[k])), cmul(ph, hi2(A[k])));
+  }
+}
+
+struct GroupArgs {
+  uint32_t pos[5];  // vector-bit positions of the wires >= 1, ascending
+  M2 m[5];          // their matrices
+  M2 m0;            // matrix of wire 0 when W0
+};
+
+// KP wires >= 1 (plus wire 0 when W0): a site owns 2^KP vectors in registers.
+template <int KP, bool W0>
+__global__ void __launch_bounds__(kThreads)
+k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
+  constexpr int NV = 1 << KP;
+  const uint64_t s = static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x;
+  if (s >= nsites) return;
+  uint64_t base = s;
+#pragma unroll
+  for (int j = 0; j < KP; j++) base = ins0(base, g.pos[j]);
+  float4 r[NV];
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    uint64_t v = base;
+#pragma unroll
+    for (int j = 0; j < KP; j++)
+      if ((l >> j) & 1) v |= 1ull << g.pos[j];
+    r[l] = st[v];
+  }
+  if (W0) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      float2 x = lo2(r[l]), y = hi2(r[l]);
+      apply2(g.m0, x, y);
+      r[l] = pack4(x, y);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < KP; j++) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      if ((l >> j) & 1) continue;
+      const int h = l | (1 << j);
+      float2 a0 = lo2(r[l]), b0 = lo2(r[h]), a1 = hi2(r[l]), b1 = hi2(r[h]);
+      apply2(g.m[j], a0, b0);
+      apply2(g.m[j], a1, b1);
+      r[l] = pack4(a0, a1);
+      r[h] = pack4(b0, b1);
+    }
+  }
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    uint64_t v = base;
+#pragma unroll
+    for (int j = 0; j < KP; j++)
+      if ((l >> j) & 1) v |= 1ull << g.pos[j];
+    st[v] = r[l];
+  }
+}
+
+constexpr int kMaxBlockedGates = 96;
+struct BlockedArgs {
+  uint32_t count;
+  uint8_t q[kMaxBlockedGates];
+  M2 m[kMaxBlockedGates];
+};
+
+// One CTA per 2^b block: stage it in shared memory, apply every gate in
+// order with a barrier between gates, write it back once.
+__global__ void __launch_bounds__(kThreads)
+k_blocked(float2 *__restrict__ st, uint32_t b, uint64_t nblocks, BlockedArgs g) {
+  extern __shared__ float4 smem4[];
+  float2 *tile = reinterpret_cast<float2 *>(smem4);
+  const uint32_t block = 1u << b;
+  const uint32_t pairs = block >> 1;
+  for (uint64_t blk = blockIdx.x; blk < nblocks; blk += gridDim.x) {
+    const uint64_t base = blk << b;
+    const float4 *src = reinterpret_cast<const float4 *>(st + base);
+    for (uint32_t i = threadIdx.x; i < block / 2; i += kThreads) smem4[i] = src[i];
+    __syncthreads();
+    for (uint32_t k = 0; k < g.count; k++) {
+      const uint32_t q = g.q[k], stride = 1u << q;
+      const M2 m = g.m[k];
+      for (uint32_t t = threadIdx.x; t < pairs; t += kThreads) {
+        const uint32_t i = ((t >> q) << (q + 1)) | (t & (stride - 1));
+        float2 x = tile[i], y = tile[i + stride];
+        apply2(m, x, y);
+        tile[i] = x;
+        tile[i + stride] = y;
+      }
+      __syncthreads();
+    }
+    float4 *dst = reinterpret_cast<float4 *>(st + base);
+    for (uint32_t i = threadIdx.x; i < block / 2; i += kThreads) dst[i] = smem4[i];
+    __syncthreads();
+  }
+}
+
+// Swap for wires a < b. A0: a == 0, so lane z,w of vector v (a=1,b=0) trades
+// with lanes x,y of v|tb (a=0,b=1). Otherwise whole vectors trade.
+template <bool A0>
+__global__ void __launch_bounds__(kThreads)
+k_swap(float4 *__restrict__ st, uint64_t nsites, Fix f, uint64_t ta, uint64_t tb) {
+#pragma unroll
+  for (int k = 0; k < U; k++) {
+    const uint64_t s = site_of(k);
+    if (s >= nsites) continue;
+    const uint64_t v = expand(s, f);
+    if (A0) {
+      float4 A = st[v], B = st[v | tb];
+      st[v] = make_float4(A.x, A.y, B.x, B.y);
+      st[v | tb] = make_float4(A.z, A.w, B.z, B.w);
+    } else {
+      const float4 A = st[v | ta], B = st[v | tb];
+      st[v | ta] = B;
+      st[v | tb] = A;
+    }
+  }
+}
+
+Fix make_fix(std::vector<uint32_t> pos, uint64_t set) {
+  std::sort(pos.begin(), pos.end());
+  Fix f{};
+  f.nfix = static_cast<uint32_t>(pos.size());
+  for (size_t j = 0; j < pos.size(); j++) f.pos[j] = pos[j];
+  f.set = set;
+  return f;
+}
+
+bool valid_state(const float *p, uint32_t n) {
+  return p && n >= 1 && n <= 40 && (reinterpret_cast<uintptr_t>(p) & 15u) == 0;
+}
+
+}  // namespace
+
+namespace qmk_host {
+int num_sms() {
+  static int cache[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
+  if (!cache[dev]) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    cache[dev] = v > 0 ? v : 148;
+  }
+  return cache[dev];
+}
+}  // namespace qmk_host
+
+using qmk_host::grid_for;
+using qmk_host::launch_status;
+
+extern "C" int qmk_init_basis(float *state, uint32_t n, void *stream) {
+  if (!valid_state(state, n)) return -1;
+  const uint64_t nvec = 1ull << (n - 1);
+  k_init_basis<<<grid_for(nvec, kThreads * U), kThreads, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<float4 *>(state), nvec);
+  return launch_status();
+}
+
+// Shared launcher for the controlled family (no controls == dense 2x2).
+static int launch_controlled(float *state, uint32_t n, const uint32_t *ctrl,
+                             uint32_t nctrl, uint32_t t, const float m8[8],
+                             cudaStream_t stream) {
+  if (!valid_state(state, n) || t >= n || nctrl > 2) return -1;
+  bool ctrl0 = false;
+  std::vector<uint32_t> pos;
+  uint64_t set = 0;
+  for (uint32_t j = 0; j < nctrl; j++) {
+    if (ctrl[j] >= n || ctrl[j] == t) return -1;
+    for (uint32_t k = 0; k < j; k++)
+      if (ctrl[k] == ctrl[j]) return -1;
+    if (ctrl[j] == 0) {
+      ctrl0 = true;
+    } else {
+      pos.push_back(ctrl[j] - 1);
+      set |= 1ull << (ctrl[j] - 1);
+    }
+  }
+  const M2 m = m2_from(m8);
+  float4 *st = reinterpret_cast<float4 *>(state);
+  if (t == 0) {
+    const Fix f = make_fix(pos, set);
+    const uint64_t nsites = 1ull << (n - 1 - f.nfix);
+    k_pair<0><<<grid_for(nsites, kThreads * U), kThreads, 0, stream>>>(st, nsites, f, 0, m);
+    return launch_status();
+  }
+  pos.push_back(t - 1);
+  const Fix f = make_fix(pos, set);
+  if (n - 1 < f.nfix) return -1;
+  const uint64_t nsites = 1ull << (n - 1 - f.nfix);
+  const uint64_t tbit = 1ull << (t - 1);
+  if (ctrl0)
+    k_pair<2><<<grid_for(nsites, kThreads * U), kThreads, 0, stream>>>(st, nsites, f, tbit, m);
+  else
+    k_pair<1><<<grid_for(nsites, kThreads * U), kThreads, 0, stream>>>(st, nsites, f, tbit, m);
+  return launch_status();
+}
+
+extern "C" int qmk_apply_1q(float *state, uint32_t n, uint32_t q,
+                            const float m[8], void *stream) {
+  return launch_controlled(state, n, nullptr, 0, q, m, (cudaStream_t)stream);
+}
+
+extern "C" int qmk_apply_controlled(float *state, uint32_t n,
+                                    uint32_t num_controls,
+                                    const uint32_t *controls, uint32_t target,
+                                    const float m[8], void *stream) {
+  if (num_controls < 1 || num_controls > 2 || !controls) return -1;
+  return launch_controlled(state, n, controls, num_controls, target, m,
+                           (cudaStream_t)stream);
+}
+
+extern "C" int qmk_apply_phase(float *state, uint32_t n, uint64_t mask,
+                               float re, float im, void *stream) {
+  if (!valid_state(state, n) || mask == 0 || (n < 64 && (mask >> n)) ||
+      __builtin_popcountll(mask) > 3)
+    return -1;
+  std::vector<uint32_t> pos;
+  uint64_t set = 0;
+  for (uint32_t b = 1; b < n; b++)
+    if (mask >> b & 1) {
+      pos.push_back(b - 1);
+      set |= 1ull << (b - 1);
+    }
+  const Fix f = make_fix(pos, set);
+  const uint64_t nsites = 1ull << (n - 1 - f.nfix);
+  const float2 ph = make_float2(re, im);
+  float4 *st = reinterpret_cast<float4 *>(state);
+  if (mask & 1)
+    k_phase<true><<<grid_for(nsites, kThreads * U), kThreads, 0, (cudaStream_t)stream>>>(st, nsites, f, ph);
+  else
+    k_phase<false><<<grid_for(nsites, kThreads * U), kThreads, 0, (cudaStream_t)stream>>>(st, nsites, f, ph);
+  return launch_status();
+}
+
+template <int KP, bool W0>
+static void launch_group(float4 *st, uint64_t nsites, const GroupArgs &g,
+                         cudaStream_t stream) {
+  k_group<KP, W0><<<grid_for(nsites, kThreads), kThreads, 0, stream>>>(st, nsites, g);
+}
+
+extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
+                               const uint32_t *qubits, const float *mats,
+                               void *stream) {
+  if (!valid_state(state, n) || k < 1 || k > 5 || !qubits || !mats) return -1;
+  for (uint32_t j = 0; j < k; j++) {
+    if (qubits[j] >= n) return -1;
+    if (j && qubits[j] <= qubits[j - 1]) return -1;  // ascending, distinct
+  }
+  GroupArgs g{};
+  const bool w0 = qubits[0] == 0;
+  int kp = 0;
+  for (uint32_t j = 0; j < k; j++) {
+    if (qubits[j] == 0) {
+      g.m0 = m2_from(mats + 8 * j);
+    } else {
+      g.pos[kp] = qubits[j] - 1;
+      g.m[kp] = m2_from(mats + 8 * j);
+      kp++;
+    }
+  }
+  if (static_cast<uint32_t>(kp) > n - 1) return -1;
+  const uint64_t nsites = 1ull << (n - 1 - kp);
+  float4 *st = reinterpret_cast<float4 *>(state);
+  cudaStream_t s = (cudaStream_t)stream;
+  switch (kp * 2 + (w0 ? 1 : 0)) {
+    case 1: launch_group<0, true>(st, nsites, g, s); break;
+    case 2: launch_group<1, false>(st, nsites, g, s); break;
+    case 3: launch_group<1, true>(st, nsites, g, s); break;
+    case 4: launch_group<2, false>(st, nsites, g, s); break;
+    case 5: launch_group<2, true>(st, nsites, g, s); break;
+    case 6: launch_group<3, false>(st, nsites, g, s); break;
+    case 7: launch_group<3, true>(st, nsites, g, s); break;
+    case 8: launch_group<4, false>(st, nsites, g, s); break;
+    case 9: launch_group<4, true>(st, nsites, g, s); break;
+    case 10: launch_group<5, false>(st, nsites, g, s); break;
+    default: return -1;
+  }
+  return launch_status();
+}
+
+extern "C" int qmk_apply_blocked(float *state, uint32_t n, uint32_t b,
+                                 uint32_t count, const uint32_t *qubits,
+                                 const float *mats, void *stream) {
+  if (!valid_state(state, n) || b < 2 || b > 14 || b > n) return -1;
+  if (count && (!qubits || !mats)) return -1;
+  for (uint32_t k = 0; k < count; k++)
+    if (qubits[k] >= b) return -1;
+  const size_t smem = sizeof(float2) << b;
+  if (smem > 48 * 1024) {
+    cudaError_t e = cudaFuncSetAttribute(k_blocked, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+  }
+  const uint64_t nblocks = 1ull << (n - b);
+  // Runs longer than one argument block go in consecutive passes; each pass
+  // applies its gates in order, so the composition is unchanged.
+  uint32_t done = 0;
+  do {
+    BlockedArgs g{};
+    g.count = std::min<uint32_t>(count - done, kMaxBlockedGates);
+    for (uint32_t k = 0; k < g.count; k++) {
+      g.q[k] = static_cast<uint8_t>(qubits[done + k]);
+      g.m[k] = m2_from(mats + 8 * (done + k));
+    }
+    const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(nblocks, 1u << 20));
+    k_blocked<<<grid, kThreads, smem, (cudaStream_t)stream>>>(
+        reinterpret_cast<float2 *>(state), b, nblocks, g);
+    int rc = launch_status();
+    if (rc) return rc;
+    done += g.count;
+  } while (done < count);
+  return 0;
+}
+
+extern "C" int qmk_apply_swap(float *state, uint32_t n, uint32_t a, uint32_t b,
+                              void *stream) {
+  if (!valid_state(state, n) || a >= n || b >= n) return -1;
+  if (a == b) return 0;
+  if (a > b) std::swap(a, b);
+  float4 *st = reinterpret_cast<float4 *>(state);
+  cudaStream_t s = (cudaStream_t)stream;
+  if (a == 0) {
+    const Fix f = make_fix({b - 1}, 0);
+    const uint64_t nsites = 1ull << (n - 2);
+    k_swap<true><<<grid_for(nsites, kThreads * U), kThreads, 0, s>>>(st, nsites, f, 0, 1ull << (b - 1));
+  } else {
+    const Fix f = make_fix({a - 1, b - 1}, 0);
+    const uint64_t nsites = 1ull << (n - 3);
+    k_swap<false><<<grid_for(nsites, kThreads * U), kThreads, 0, s>>>(
+        st, nsites, f, 1ull << (a - 1), 1ull << (b - 1));
+  }
+  return launch_status();
+}

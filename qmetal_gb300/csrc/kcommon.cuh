@@ -1,0 +1,110 @@
+// kcommon.cuh -- shared device helpers for the statevector kernels.
+//
+// Layout: the state is 2^n complex64 amplitudes, interleaved, LSB-first.
+// Most kernels address it as float4 "vectors": vector v holds amplitudes 2v
+// (lanes x,y) and 2v+1 (lanes z,w), so amplitude bit 0 is the lane and
+// amplitude bit b >= 1 is vector bit b-1. Every global access is then a
+// 16-byte load or store, and a warp touches 512 contiguous bytes whenever
+// the vector bits below 5 are free.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace qmk {
+
+constexpr int kThreads = 256;
+
+struct M2 {
+  float2 a, b, c, d;  // [[a b] [c d]]
+};
+
+__host__ inline M2 m2_from(const float m[8]) {
+  M2 r;
+  r.a = make_float2(m[0], m[1]);
+  r.b = make_float2(m[2], m[3]);
+  r.c = make_float2(m[4], m[5]);
+  r.d = make_float2(m[6], m[7]);
+  return r;
+}
+
+__device__ __forceinline__ float2 cmul(float2 x, float2 y) {
+  return make_float2(x.x * y.x - x.y * y.y, x.x * y.y + x.y * y.x);
+}
+
+// m0 * u + m1 * v
+__device__ __forceinline__ float2 cmac2(float2 m0, float2 u, float2 m1, float2 v) {
+  return make_float2(m0.x * u.x - m0.y * u.y + m1.x * v.x - m1.y * v.y,
+                     m0.x * u.y + m0.y * u.x + m1.x * v.y + m1.y * v.x);
+}
+
+__device__ __forceinline__ void apply2(const M2 &m, float2 &u, float2 &v) {
+  const float2 nu = cmac2(m.a, u, m.b, v);
+  const float2 nv = cmac2(m.c, u, m.d, v);
+  u = nu;
+  v = nv;
+}
+
+__device__ __forceinline__ float2 lo2(const float4 &x) { return make_float2(x.x, x.y); }
+__device__ __forceinline__ float2 hi2(const float4 &x) { return make_float2(x.z, x.w); }
+__device__ __forceinline__ float4 pack4(float2 a, float2 b) {
+  return make_float4(a.x, a.y, b.x, b.y);
+}
+
+// Insert a zero bit at position p (bits >= p move up one).
+__device__ __forceinline__ uint64_t ins0(uint64_t x, uint32_t p) {
+  const uint64_t low = x & ((1ull << p) - 1ull);
+  return ((x >> p) << (p + 1)) | low;
+}
+
+__device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
+
+// e^{i phi} for an angle summed in FP64: reduced to [-pi, pi] in FP64, then
+// evaluated with the single-precision sincosf (about 1 ulp there).
+__device__ __forceinline__ float2 expi_reduced(double phi) {
+  const double two_pi = 6.283185307179586476925286766559;
+  const double k = rint(phi * (1.0 / two_pi));
+  const double r = fma(-k, two_pi, phi);
+  float s, c;
+  sincosf(static_cast<float>(r), &s, &c);
+  return make_float2(c, s);
+}
+
+// FP64 warp sum.
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Block of kThreads threads; returns the block sum in thread 0 (other threads
+// get unspecified values). `sm` needs kThreads/32 doubles.
+__device__ __forceinline__ double block_sum(double v, double *sm) {
+  v = warp_sum(v);
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if (l == 0) sm[w] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (w == 0) {
+    r = (l < kThreads / 32) ? sm[l] : 0.0;
+    r = warp_sum(r);
+  }
+  __syncthreads();
+  return r;
+}
+
+}  // namespace qmk
+
+// Device / grid helpers shared by the launchers (host side).
+namespace qmk_host {
+int num_sms();
+inline unsigned grid_for(uint64_t items, uint64_t per_block) {
+  uint64_t g = (items + per_block - 1) / per_block;
+  if (g == 0) g = 1;
+  return static_cast<unsigned>(g);
+}
+inline int launch_status() {
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? 0 : static_cast<int>(e);
+}
+}  // namespace qmk_host

@@ -1,0 +1,96 @@
+// simulator.hpp -- the statevector executor on one CUDA device.
+//
+// Same surface as the reference's C++ Simulator (include/qmetal/simulator.h:
+// 30-112) so the C ABI maps onto it one to one; the implementation owns a
+// device state buffer, a stream, a scratch workspace, and launches the
+// sm_103a kernels declared in include/qmetal/qmetal_kernels.h.
+#pragma once
+
+#include <cstdint>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "circuit.hpp"
+
+namespace qmetal {
+
+// 34 qubits = 128 GiB of complex64, in place, fits one GB300's HBM.
+constexpr uint32_t kMaxQubits = 34;
+
+class Simulator {
+ public:
+  explicit Simulator(uint32_t num_qubits);
+  ~Simulator();
+  Simulator(const Simulator &) = delete;
+  Simulator &operator=(const Simulator &) = delete;
+
+  void reset();
+  void apply(const Gate &g);
+  void run(const Circuit &c);
+  void run(const Circuit &c, const FusionOptions &opts);
+  void run(const Plan &p);
+  void apply(const PlanOp &op);
+  // Runs the plan with a CUDA event between ops; seconds[i] = op i's device time.
+  void run_profiled(const Plan &p, std::vector<double> &seconds);
+  void synchronize();
+
+  uint32_t num_qubits() const { return n_; }
+  size_t dim() const { return size_t(1) << n_; }
+
+  const float *raw();                   // host mirror, refreshed
+  void get_state(float *out);           // 2 * dim floats
+  void set_state(const float *in);      // 2 * dim floats
+
+  double abs2sum();
+  double norm();
+  double expectation(const PauliString &p);
+  double expectation(const Hamiltonian &h);
+  void expectation_terms(const Hamiltonian &h, double *out);
+
+  std::vector<uint64_t> sample(size_t shots, uint64_t seed = 0);
+
+  std::pair<double, std::vector<double>> energy_and_gradient(const Circuit &c,
+                                                             const Hamiltonian &h);
+
+  uint64_t dispatch_count() const { return dispatches_; }
+  double elapsed();
+
+  static bool available();
+  static std::string device_name();
+  static uint64_t max_buffer_length();
+  static uint64_t recommended_working_set();
+
+ private:
+  void release();
+  void check(int rc, const char *what);
+  void activate() const;
+  void apply_gate_to(float *state, const Gate &g);
+  void apply_op_to(float *state, const PlanOp &op);
+  void pauli_values(const float *state, const Hamiltonian &h, std::vector<double> &vals);
+  void costate(const Hamiltonian &h);
+  void fetch(size_t count);             // d_results_ -> h_results_, sync
+
+  uint32_t n_ = 0;
+  int device_ = 0;
+  void *stream_ = nullptr;
+  float *state_ = nullptr;
+  float *costate_ = nullptr;
+  void *ws_ = nullptr;
+  size_t ws_bytes_ = 0;
+  void *sample_ws_ = nullptr;
+  size_t sample_ws_bytes_ = 0;
+  uint64_t *d_shots_ = nullptr;
+  size_t d_shots_cap_ = 0;
+  double *d_results_ = nullptr;         // kResultSlots doubles
+  double *h_results_ = nullptr;         // pinned mirror
+  double *d_grad_ = nullptr;            // adjoint gradient slots
+  size_t d_grad_cap_ = 0;
+  float *mirror_ = nullptr;
+  bool mirror_pinned_ = false;
+  void *ev_start_ = nullptr, *ev_stop_ = nullptr;
+  uint64_t dispatches_ = 0;
+  bool fault_launch_ = false;
+};
+
+}  // namespace qmetal

@@ -1,0 +1,98 @@
+"""The C boundary, without a GPU.
+
+The library loads, exports every symbol that include/qmetal/*.h declares,
+the public header is valid C11, and every failure path reports through the
+return code and qm_last_error() rather than crashing (src/capi.cpp:19-38).
+"""
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+import qmetal_gb300 as qm
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADERS = [os.path.join(ROOT, "include", "qmetal", h) for h in ("qmetal.h", "qmetal_kernels.h")]
+
+
+def declared(path):
+    text = open(path).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(qmk?_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_every_declared_symbol_is_exported():
+    lib = ctypes.CDLL(qm.library_path())
+    missing = [s for h in HEADERS for s in declared(h) if not hasattr(lib, s)]
+    assert not missing, missing
+    assert len(declared(HEADERS[0])) >= 30 and len(declared(HEADERS[1])) >= 15
+
+
+@pytest.mark.parametrize("header", HEADERS)
+def test_header_is_plain_c11(header, tmp_path):
+    src = tmp_path / "t.c"
+    src.write_text(f'#include "{header}"\nint main(void) {{ return 0; }}\n')
+    subprocess.run(["gcc", "-std=c11", "-Wall", "-Wextra", "-Werror", "-pedantic",
+                    "-fsyntax-only", str(src)], check=True)
+
+
+def test_gate_codes_are_the_reference_numbering():
+    assert (qm.X, qm.Y, qm.Z, qm.H, qm.S, qm.SDG, qm.T, qm.TDG) == tuple(range(8))
+    assert (qm.RX, qm.RY, qm.RZ, qm.P, qm.CX, qm.CY, qm.CZ, qm.SWAP, qm.CP, qm.CCX) == \
+        tuple(range(8, 18))
+
+
+def test_diagnostics():
+    assert qm.version() == (0, 1, 0)
+    assert qm.max_qubits() == 34
+    assert isinstance(qm.is_available(), bool)
+    assert isinstance(qm.device_name(), str)
+
+
+def test_circuit_errors_cross_as_exceptions():
+    with pytest.raises(qm.QMetalError, match="out of range"):
+        qm.Circuit(2).x(5)
+    with pytest.raises(qm.QMetalError, match="arity"):
+        qm.Circuit(2).add(qm.X, ())
+    with pytest.raises(qm.QMetalError, match="unknown gate"):
+        qm.Circuit(2).add(99, (0,))
+    c = qm.Circuit(3)
+    c.h(0).cx(0, 1).ccx(0, 1, 2)
+    assert len(c) == 3 and c.plan_size(fuse=False) == 3
+
+
+def test_unsupported_gate_fails_plan_closed():
+    c = qm.Circuit(2)
+    c.add(qm.X, (0, 1))           # a one-qubit kind given two wires
+    assert c.plan_size() == 0     # size query reports 0 ...
+    lib = ctypes.CDLL(qm.library_path())
+    lib.qm_last_error.restype = ctypes.c_char_p
+    assert b"unsupported" in lib.qm_last_error()   # ... and leaves the message
+
+
+@pytest.mark.skipif(qm.is_available(), reason="checks the no-device path")
+def test_no_device_fails_closed():
+    with pytest.raises(qm.QMetalError):
+        qm.Simulator(4)
+
+
+def test_null_handles_are_rejected():
+    lib = ctypes.CDLL(qm.library_path())
+    lib.qm_run.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.qm_norm.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
+    lib.qm_last_error.restype = ctypes.c_char_p
+    assert lib.qm_run(None, None) == -1
+    assert b"null" in lib.qm_last_error()
+    assert lib.qm_norm(None, None) == -1
+
+
+def test_kernel_layer_rejects_bad_arguments_without_launching():
+    lib = ctypes.CDLL(qm.library_path())
+    f = lib.qmk_apply_1q
+    f.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_void_p]
+    m = (ctypes.c_float * 8)()
+    assert f(None, 4, 0, m, None) == -1                      # null state
+    assert f(ctypes.c_void_p(16), 4, 9, m, None) == -1       # wire out of range
+    assert f(ctypes.c_void_p(18), 4, 0, m, None) == -1       # misaligned
