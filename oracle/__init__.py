@@ -8,7 +8,10 @@ Two backends:
   * ``libqoracle.so`` -- qsim_oracle.c, a plain-C complex128 restatement of
     the reference's CPU oracle (src/reference.cpp) plus its sampling and
     adjoint algorithms (src/metal/simulator.mm:677-763, 782-963). Built by
-    ``build()`` from source on whatever machine runs the tests.
+    ``build()`` from source on whatever machine runs the tests. Gate loops
+    run on OpenMP threads above 2^16 amplitudes (bit-identical to a serial
+    run: every iteration writes its own elements); OMP_NUM_THREADS=1 gives
+    the reference's single-thread behaviour.
   * ``_ref/libqref.so`` -- the reference project's own CPU sources compiled
     by build_ref.sh (only where those sources exist). Used to pin the
     restatement and the library's plan builder; absent elsewhere.
@@ -40,8 +43,8 @@ def build() -> str:
     if os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(src):
         return LIB
     tmp = LIB + ".tmp"
-    subprocess.run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", src, "-o", tmp, "-lm"],
-                   check=True)
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-fopenmp", src, "-o", tmp,
+                    "-lm"], check=True)
     os.replace(tmp, LIB)
     return LIB
 

@@ -33,6 +33,14 @@
 
 typedef double _Complex cplx;
 
+/* Gate loops write disjoint elements, so splitting them across threads does
+ * not change a single bit of the result; small states stay serial. */
+#define PAR_MIN ((uint64_t)1 << 16)
+#define PARALLEL_FOR(count)                                                  \
+  const uint64_t par_n = (count);                                            \
+  (void)par_n;                                                               \
+  _Pragma("omp parallel for schedule(static) if (par_n >= PAR_MIN)")
+
 enum {
   K_X = 0, K_Y, K_Z, K_H, K_S, K_SDG, K_T, K_TDG,
   K_RX, K_RY, K_RZ, K_P,
@@ -97,6 +105,7 @@ int qo_gate_matrix(int kind, const double *params, double out[8]) {
 
 static void apply_1q(cplx *st, uint64_t dim, uint32_t q, const cplx m[4]) {
   const uint64_t stride = (uint64_t)1 << q, pairs = dim >> 1;
+  PARALLEL_FOR(pairs)
   for (uint64_t t = 0; t < pairs; t++) {
     uint64_t i = ((t >> q) << (q + 1)) | (t & (stride - 1));
     uint64_t j = i | stride;
@@ -109,6 +118,7 @@ static void apply_1q(cplx *st, uint64_t dim, uint32_t q, const cplx m[4]) {
 static void apply_ctrl_1q(cplx *st, uint64_t dim, uint32_t c, uint32_t t,
                           const cplx m[4]) {
   const uint64_t cm = (uint64_t)1 << c, tm = (uint64_t)1 << t;
+  PARALLEL_FOR(dim)
   for (uint64_t i = 0; i < dim; i++) {
     if (!(i & cm) || (i & tm)) continue;
     uint64_t j = i | tm;
@@ -121,6 +131,7 @@ static void apply_ctrl_1q(cplx *st, uint64_t dim, uint32_t c, uint32_t t,
 static void apply_diag_2q(cplx *st, uint64_t dim, uint32_t a, uint32_t b,
                           cplx ph) {
   const uint64_t ma = (uint64_t)1 << a, mb = (uint64_t)1 << b;
+  PARALLEL_FOR(dim)
   for (uint64_t i = 0; i < dim; i++)
     if ((i & ma) && (i & mb)) st[i] *= ph;
 }
@@ -128,6 +139,7 @@ static void apply_diag_2q(cplx *st, uint64_t dim, uint32_t a, uint32_t b,
 static void apply_swap(cplx *st, uint64_t dim, uint32_t a, uint32_t b) {
   if (a == b) return;
   const uint64_t ma = (uint64_t)1 << a, mb = (uint64_t)1 << b;
+  PARALLEL_FOR(dim)
   for (uint64_t i = 0; i < dim; i++) {
     if ((i & ma) && !(i & mb)) {
       uint64_t j = (i ^ ma) | mb;
@@ -140,6 +152,7 @@ static void apply_ccx(cplx *st, uint64_t dim, uint32_t c0, uint32_t c1,
                       uint32_t t) {
   const uint64_t m0 = (uint64_t)1 << c0, m1 = (uint64_t)1 << c1,
                  mt = (uint64_t)1 << t;
+  PARALLEL_FOR(dim)
   for (uint64_t i = 0; i < dim; i++) {
     if ((i & m0) && (i & m1) && !(i & mt)) {
       cplx x = st[i]; st[i] = st[i | mt]; st[i | mt] = x;
@@ -242,6 +255,7 @@ int qo_run_plan(uint32_t n, double *state, const double *plan, size_t len) {
       case OP_SWAP: apply_swap(st, dim, q0, q1); break;
       case OP_CCX: apply_ccx(st, dim, q0, q1, q2); break;
       case OP_DIAG:
+        PARALLEL_FOR(dim)
         for (uint64_t i = 0; i < dim; i++) {
           double phi = gphase;
           for (size_t t = 0; t < nt; t++) {
@@ -399,6 +413,7 @@ static cplx ipow(unsigned ny) {
 /* dst += c * (P src), (P src)_i = sgn(i ^ flip) * src_{i ^ flip} */
 static void pauli_accum(cplx *dst, const cplx *src, uint64_t dim,
                         uint64_t flip, uint64_t sign, cplx c) {
+  PARALLEL_FOR(dim)
   for (uint64_t i = 0; i < dim; i++) {
     uint64_t j = i ^ flip;
     double s = (__builtin_popcountll(j & sign) & 1) ? -1.0 : 1.0;

@@ -1,0 +1,186 @@
+"""GPU checks at the benchmark configurations' sizes.
+
+1. QFT + swap layer at 22 qubits, gate by gate, from a seeded random
+   normalised state: every amplitude against the complex128 oracle.
+2. The four fused 30-qubit workloads, checked against the oracle at 20 and 26
+   qubits (fused and gate by gate), and their norms at 30.
+3. GHZ and QFT at 33 and 34 qubits without an oracle: norm, <Z_q>, GHZ
+   <Z_0 Z_{n-1}> and 10^6 samples landing only on the two poles.
+4. Adjoint gradients of the HEA depth-8 problem through torch.autograd:
+   parameter shift on the oracle, central differences on the GPU.
+"""
+import math
+
+import numpy as np
+import pytest
+
+import oracle
+import qmetal_gb300 as qm
+from qmetal_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+def random_state(n, seed):
+    rng = np.random.default_rng(seed)
+    v = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    return (v / np.linalg.norm(v)).astype(np.complex64)
+
+
+@pytest.mark.parametrize("fuse", [False, True])
+def test_qft22_gate_by_gate_from_random_state(fuse):
+    n = 22
+    init = random_state(n, 22)
+    gates = W.qft_swap(n)
+    assert len(gates) == 22 + 231 + 11
+    c = W.to_circuit(n, gates)
+    sim = qm.Simulator(n)
+    sim.set_state(init)
+    sim.run(c, fuse=fuse)
+    want = oracle.run(n, gates, init.astype(np.complex128))
+    got = sim.get_state()
+    err = np.abs(got - want).max()
+    assert err <= 1e-5, err
+    # relative to the amplitude scale, too
+    assert err / np.abs(want).max() <= 1e-4
+
+
+WORKLOADS = {
+    "qaoa_ring_p6": lambda n: W.qaoa_ring_seeded(n, 6, seed=1),
+    "tfim_trotter_20": lambda n: W.tfim_chain(n, 20, 1.0, 0.7, 0.05),
+    "hea_d3": lambda n: W.hea(n, 3, seed=3),
+    "random_u3_d10": lambda n: W.random_u3(n, 10, seed=4),
+}
+
+
+@pytest.mark.parametrize("name", list(WORKLOADS))
+@pytest.mark.parametrize("n", [20, 26])
+def test_fused_workloads_vs_oracle(name, n):
+    gates = WORKLOADS[name](n)
+    want = oracle.run(n, gates)
+    c = W.to_circuit(n, gates)
+    sim = qm.Simulator(n)
+    for fuse in (True, False):
+        sim.reset()
+        sim.run(c, fuse=fuse)
+        err = np.abs(sim.get_state() - want).max()
+        assert err <= 1e-5, (fuse, err)
+
+
+@pytest.mark.parametrize("name", list(WORKLOADS))
+def test_fused_workloads_norm_at_30(name):
+    n = 30
+    sim = qm.Simulator(n)
+    sim.run(W.to_circuit(n, WORKLOADS[name](n)))
+    assert abs(sim.norm() - 1.0) <= 1e-4
+
+
+@pytest.mark.parametrize("n", [33, 34])
+def test_scale_ghz(n):
+    sim = qm.Simulator(n)
+    sim.run(W.to_circuit(n, W.ghz(n)))
+    assert abs(sim.norm() - 1.0) <= 1e-4
+    for q in (0, n // 2, n - 1):
+        assert abs(sim.expectation_pauli(z_mask=1 << q)) <= 1e-4
+    assert abs(sim.expectation_pauli(z_mask=1 | (1 << (n - 1))) - 1.0) <= 1e-4
+    shots = np.array(sim.sample(1_000_000, 7), dtype=np.uint64)
+    ones = (1 << n) - 1
+    assert np.all((shots == 0) | (shots == ones))
+    assert abs(np.mean(shots == 0) - 0.5) < 0.005
+
+
+@pytest.mark.parametrize("n", [33, 34])
+def test_scale_qft(n):
+    sim = qm.Simulator(n)
+    sim.run(W.to_circuit(n, W.qft(n)))
+    assert abs(sim.norm() - 1.0) <= 1e-3
+    for q in range(0, n, max(1, n // 8)):
+        assert abs(sim.expectation_pauli(z_mask=1 << q)) <= 1e-3
+    shots = np.array(sim.sample(1_000_000, 11), dtype=np.uint64)
+    # uniform: every bit is a fair coin
+    bits = [(np.mean((shots >> np.uint64(q)) & np.uint64(1))) for q in (0, n // 2, n - 1)]
+    assert all(abs(b - 0.5) < 0.005 for b in bits)
+
+
+def _shift(n, gates, terms, k):
+    kind, qs, ps = gates[k]
+    plus = list(gates); plus[k] = (kind, qs, (ps[0] + math.pi / 2,))
+    minus = list(gates); minus[k] = (kind, qs, (ps[0] - math.pi / 2,))
+    return 0.5 * (oracle.expectation_sum(n, oracle.run(n, plus), terms)
+                  - oracle.expectation_sum(n, oracle.run(n, minus), terms))
+
+
+def test_autograd_hea_d8_vs_parameter_shift_n12():
+    torch = pytest.importorskip("torch")
+    from qmetal_gb300.autograd import Template, energy
+    n = 12
+    gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
+    tpl = Template(n, gates)
+    assert tpl.num_params == 2 * n * 8
+    theta = torch.tensor(tpl.angles(), dtype=torch.float64, requires_grad=True)
+    e = energy(theta, tpl, terms)
+    e.backward()
+    assert abs(e.item() - oracle.expectation_sum(n, oracle.run(n, gates), terms)) <= 1e-5
+    want = np.array([_shift(n, gates, terms, k) for k in tpl.param_index])
+    assert np.abs(theta.grad.numpy() - want).max() <= 1e-5
+
+
+def test_autograd_hea_d8_subset_vs_parameter_shift_n20():
+    torch = pytest.importorskip("torch")
+    from qmetal_gb300.autograd import Template, energy
+    n = 20
+    gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
+    tpl = Template(n, gates)
+    theta = torch.tensor(tpl.angles(), dtype=torch.float64, requires_grad=True)
+    energy(theta, tpl, terms).backward()
+    rng = np.random.default_rng(0)
+    for j in rng.choice(tpl.num_params, size=6, replace=False):
+        want = _shift(n, gates, terms, tpl.param_index[j])
+        assert abs(theta.grad[j].item() - want) <= 1e-5, j
+
+
+def test_autograd_central_differences_and_chain_rule():
+    torch = pytest.importorskip("torch")
+    from qmetal_gb300.autograd import Template, energy
+    n = 16
+    gates, terms = W.hea_gradient_problem(n, depth=8, seed=9)
+    tpl = Template(n, gates)
+    sim = qm.Simulator(n)
+    base = torch.tensor(tpl.angles(), dtype=torch.float64)
+    # a tied parameterisation: every angle = 2 * phi_layer[k] + base, so the
+    # chain rule from autograd must sum the per-gate adjoint entries
+    phi = torch.zeros(8, dtype=torch.float64, requires_grad=True)
+    layer_of = torch.tensor([i // (2 * n) for i in range(tpl.num_params)])
+    e = energy(base + 2.0 * phi[layer_of], tpl, terms, sim)
+    e.backward()
+    eps = 1e-3
+    for k in range(8):
+        d = torch.zeros(8, dtype=torch.float64)
+        d[k] = eps
+        ep = energy(base + 2.0 * (d[layer_of]), tpl, terms, sim).item()
+        em = energy(base - 2.0 * (d[layer_of]), tpl, terms, sim).item()
+        fd = (ep - em) / (2 * eps)
+        assert abs(fd - phi.grad[k].item()) <= 2e-3 * max(1.0, abs(fd)), k
+
+
+def test_adjoint_gradient_at_28_qubits_is_consistent():
+    torch = pytest.importorskip("torch")
+    from qmetal_gb300.autograd import Template, energy
+    n = 28
+    gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
+    tpl = Template(n, gates)
+    assert tpl.num_params == 448
+    sim = qm.Simulator(n)
+    theta = torch.tensor(tpl.angles(), dtype=torch.float64, requires_grad=True)
+    e = energy(theta, tpl, terms, sim)
+    e.backward()
+    g = theta.grad.numpy()
+    assert np.isfinite(e.item()) and np.all(np.isfinite(g))
+    assert abs(e.item()) <= 2 * n
+    eps = 1e-3
+    for j in (0, 100, 447):
+        d = torch.zeros_like(theta)
+        d[j] = eps
+        fd = (energy(theta.detach() + d, tpl, terms, sim).item()
+              - energy(theta.detach() - d, tpl, terms, sim).item()) / (2 * eps)
+        assert abs(fd - g[j]) <= 5e-3, (j, fd, g[j])
