@@ -77,6 +77,22 @@ int qmk_apply_diagonal(float *state, uint32_t n, uint32_t num_terms,
                        double global_phase, void *workspace,
                        size_t workspace_bytes, void *stream);
 
+/* Returned when a size exceeds a fixed capacity (nothing is launched). */
+#define QMK_ERR_TOO_LARGE (-2)
+
+/* qmk_apply_diagonal for callers that cannot allocate device memory; no
+ * counterpart in the reference. Same arguments and result, minus the
+ * workspace: the scratch is a 327 KiB file-scope device array that every GPU
+ * loading this library holds until the process exits. Allocates nothing
+ * (no cudaMalloc / cudaFree or any allocating routine). The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress),
+ * so make that first call before any stream capture. All calls share the
+ * array: calls whose kernels may overlap on the GPU race. States above 34
+ * qubits return QMK_ERR_TOO_LARGE. */
+int qmk_apply_diagonal_noalloc(float *state, uint32_t n, uint32_t num_terms,
+                               const uint64_t *masks, const double *angles,
+                               double global_phase, void *stream);
+
 /* sum |a_i|^2 into *d_out (device double). FP32 per-thread runs, FP64 from
  * the warp up, fixed-order final sum. Replaces reduce_abs2
  * (kernels.metal:250-268; simulator.mm:615-625). */

@@ -30,7 +30,7 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
              "-I" + os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["k_gates.cu", "k_diag.cu", "k_reduce.cu", "k_sample.cu"]
+CU_SOURCES = ["k_gates.cu", "k_diag.cu", "k_reduce.cu", "k_sample.cu", "k_noalloc.cu"]
 CXX_SOURCES = ["circuit.cpp", "plan.cpp", "simulator.cpp", "capi.cpp"]
 HEADERS = ["kcommon.cuh", "circuit.hpp", "simulator.hpp"]
 PUBLIC = [os.path.join(ROOT, "include", "qmetal", "qmetal.h"),
