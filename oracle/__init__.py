@@ -85,8 +85,15 @@ def lib():
                                              c_uint32, _d, _u64, _u64, _u64, _d, _d]
         L.qo_gate_matrix.restype = c_int
         L.qo_gate_matrix.argtypes = [c_int, _d, _d]
+        L.qo_set_threads.restype = None
+        L.qo_set_threads.argtypes = [c_int]
         _lib = L
     return _lib
+
+
+def set_threads(threads: int) -> None:
+    """OpenMP threads for this process's oracle gate loops (1 = serial)."""
+    lib().qo_set_threads(int(threads))
 
 
 def ref_available() -> bool:

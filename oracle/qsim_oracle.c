@@ -206,6 +206,17 @@ int qo_run(uint32_t n, double *state, size_t ngates, const int32_t *kinds,
   return 0;
 }
 
+/* Threads for the gate loops (OpenMP); 1 reproduces the reference's
+ * single-thread oracle. */
+void qo_set_threads(int threads) {
+#ifdef _OPENMP
+  extern void omp_set_num_threads(int);
+  omp_set_num_threads(threads > 0 ? threads : 1);
+#else
+  (void)threads;
+#endif
+}
+
 void qo_reset(uint32_t n, double *state) {
   memset(state, 0, sizeof(double) * 2 * ((size_t)1 << n));
   state[0] = 1.0;

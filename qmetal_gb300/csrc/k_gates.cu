@@ -173,6 +173,103 @@ k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
   }
 }
 
+struct WarpGroupArgs {
+  uint32_t nlow;     // wires 1..5: lane bits
+  uint32_t lbit[5];  // their vector bits (0..4)
+  M2 lm[5];
+  uint32_t hpos[4];  // wires >= 6: vector bits - 5 (warp-site bits), ascending
+  M2 hm[4];
+  M2 m0;             // wire 0 (lanes) when W0
+};
+
+// Groups with wires inside one warp's 512 bytes. A warp owns 32 consecutive
+// vectors (lane = vector bits 0..4) for each combination of the KH high
+// wires, so every load and store is a full 512-byte warp access. Wire 0 is a
+// lane-pair update, wires 1..5 exchange with the partner lane by shuffle,
+// wires >= 6 pair registers. Each thread takes UW warp-sites.
+template <int KH, bool W0>
+__global__ void __launch_bounds__(kThreads)
+k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
+  constexpr int NV = 1 << KH;
+  constexpr int UW = KH <= 1 ? 4 : (KH == 2 ? 2 : 1);
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
+  uint64_t base[UW];
+  float4 r[UW][NV];
+#pragma unroll
+  for (int u = 0; u < UW; u++) {
+    const uint64_t ws = warp * UW + u;
+    base[u] = ~0ull;
+    if (ws >= nwsites) continue;
+    uint64_t b = ws;
+#pragma unroll
+    for (int j = 0; j < KH; j++) b = ins0(b, g.hpos[j]);
+    base[u] = (b << 5) | lane;
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      uint64_t v = base[u];
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      r[u][l] = st[v];
+    }
+  }
+#pragma unroll
+  for (int u = 0; u < UW; u++) {
+    // Warp-uniform: the sites of one warp are all valid or all invalid.
+    if (base[u] == ~0ull) continue;
+    if (W0) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        float2 x = lo2(r[u][l]), y = hi2(r[u][l]);
+        apply2(g.m0, x, y);
+        r[u][l] = pack4(x, y);
+      }
+    }
+#pragma unroll
+    for (int k = 0; k < 5; k++) {
+      if (k >= static_cast<int>(g.nlow)) break;
+      const uint32_t b = g.lbit[k];
+      const bool one = (lane >> b) & 1;
+      const M2 m = g.lm[k];
+      const float2 c0 = one ? m.c : m.a, c1 = one ? m.d : m.b;
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        const float4 mine = r[u][l];
+        float4 other;
+        other.x = __shfl_xor_sync(0xffffffffu, mine.x, 1 << b);
+        other.y = __shfl_xor_sync(0xffffffffu, mine.y, 1 << b);
+        other.z = __shfl_xor_sync(0xffffffffu, mine.z, 1 << b);
+        other.w = __shfl_xor_sync(0xffffffffu, mine.w, 1 << b);
+        const float4 zero_side = one ? other : mine, one_side = one ? mine : other;
+        r[u][l] = pack4(cmac2(c0, lo2(zero_side), c1, lo2(one_side)),
+                        cmac2(c0, hi2(zero_side), c1, hi2(one_side)));
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < KH; j++) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        if ((l >> j) & 1) continue;
+        const int h = l | (1 << j);
+        float2 a0 = lo2(r[u][l]), b0 = lo2(r[u][h]), a1 = hi2(r[u][l]), b1 = hi2(r[u][h]);
+        apply2(g.hm[j], a0, b0);
+        apply2(g.hm[j], a1, b1);
+        r[u][l] = pack4(a0, a1);
+        r[u][h] = pack4(b0, b1);
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      uint64_t v = base[u];
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      st[v] = r[u][l];
+    }
+  }
+}
+
 constexpr int kMaxBlockedGates = 96;
 struct BlockedArgs {
   uint32_t count;
@@ -363,8 +460,48 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
     if (qubits[j] >= n) return -1;
     if (j && qubits[j] <= qubits[j - 1]) return -1;  // ascending, distinct
   }
-  GroupArgs g{};
   const bool w0 = qubits[0] == 0;
+  cudaStream_t s = (cudaStream_t)stream;
+  float4 *st = reinterpret_cast<float4 *>(state);
+  {
+    // Wires 1..5 sit inside one warp's 512 bytes: the warp-tile kernel keeps
+    // every access a whole 512-byte warp access.
+    WarpGroupArgs wg{};
+    int kh = 0;
+    for (uint32_t j = 0; j < k; j++) {
+      const uint32_t q = qubits[j];
+      if (q == 0) {
+        wg.m0 = m2_from(mats + 8 * j);
+      } else if (q <= 5) {
+        wg.lbit[wg.nlow] = q - 1;
+        wg.lm[wg.nlow] = m2_from(mats + 8 * j);
+        wg.nlow++;
+      } else {
+        if (kh == 4) { kh = -1; break; }
+        wg.hpos[kh] = q - 6;
+        wg.hm[kh] = m2_from(mats + 8 * j);
+        kh++;
+      }
+    }
+    if (wg.nlow > 0 && kh >= 0 && n >= 6u + static_cast<uint32_t>(kh)) {
+      const uint64_t nw = 1ull << (n - 6 - kh);
+      const int uw = kh <= 1 ? 4 : (kh == 2 ? 2 : 1);
+      const unsigned grid = grid_for(nw, (kThreads / 32) * uw);
+      switch (kh * 2 + (w0 ? 1 : 0)) {
+        case 0: k_group_warp<0, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 1: k_group_warp<0, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 2: k_group_warp<1, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 3: k_group_warp<1, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 4: k_group_warp<2, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 5: k_group_warp<2, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 6: k_group_warp<3, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 7: k_group_warp<3, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        default: k_group_warp<4, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+      }
+      return launch_status();
+    }
+  }
+  GroupArgs g{};
   int kp = 0;
   for (uint32_t j = 0; j < k; j++) {
     if (qubits[j] == 0) {
@@ -377,8 +514,6 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
   }
   if (static_cast<uint32_t>(kp) > n - 1) return -1;
   const uint64_t nsites = 1ull << (n - 1 - kp);
-  float4 *st = reinterpret_cast<float4 *>(state);
-  cudaStream_t s = (cudaStream_t)stream;
   switch (kp * 2 + (w0 ? 1 : 0)) {
     case 1: launch_group<0, true>(st, nsites, g, s); break;
     case 2: launch_group<1, false>(st, nsites, g, s); break;

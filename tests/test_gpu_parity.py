@@ -127,6 +127,27 @@ def test_register_groups_all_wire_sets(k):
         assert np.abs(sim.get_state() - want).max() <= 1e-5, wires
 
 
+@pytest.mark.parametrize("k", [2, 3, 4, 5])
+def test_register_groups_with_wires_inside_a_warp(k):
+    """Groups mixing wires 0..5 (lane bits and shuffles) with up to four
+    wires >= 6 (registers), on states large enough for the warp-tile path."""
+    rng = np.random.default_rng(50 + k)
+    for n in (6, 9, 12):
+        init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+        init /= np.linalg.norm(init)
+        for trial in range(10):
+            lowq = int(rng.integers(1, 6))
+            rest = [q for q in range(n) if q != lowq]
+            wires = sorted([lowq] + rng.choice(rest, size=k - 1, replace=False).tolist())
+            gates = [(RY, (q,), (float(rng.uniform(-3, 3)),)) for q in wires]
+            gates += [(RZ, (q,), (float(rng.uniform(-3, 3)),)) for q in wires]
+            sim = qm.Simulator(n)
+            sim.set_state(init)
+            sim.run_options(W.to_circuit(n, gates), group=k)
+            want = oracle.run(n, gates, init)
+            assert np.abs(sim.get_state() - want).max() <= 1e-5, (n, wires)
+
+
 @pytest.mark.parametrize("bits", [2, 5, 8, 12])
 def test_blocked_kernel(bits, golden_circuits):
     n = 13
