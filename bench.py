@@ -237,7 +237,151 @@ def run_reference(args, world, rank, dist):
     print(json.dumps(line), flush=True)
 
 
+def run_batch_workload(args, world, rank, dist):
+    """512 QAOA MaxCut requests (n uniform over the even widths 12..26, p in
+    1..8, random 3-regular graphs, angles ~ U[0, pi]), each energy + adjoint
+    gradient + 4096 samples. A step serves the whole batch with concurrent
+    lanes; the per-circuit loop a caller of the reference API would write
+    (gate-by-gate gradient, run, sample) is timed once beside it, and so is
+    the loop with the block-wise gradient. Wall clock, host buffers."""
+    import numpy as np
+    import qmetal_gb300 as qm
+    from qmetal_gb300 import workloads as W
+    insts = W.maxcut_instances(args.requests, seed=6)
+    reqs = []
+    for k, inst in enumerate(insts):
+        gates = W.maxcut_qaoa(inst["n"], inst["edges"], inst["gammas"], inst["betas"])
+        reqs.append((W.to_circuit(inst["n"], gates),
+                     W.to_hamiltonian(W.maxcut_hamiltonian(inst["edges"])), 4096, 7000 + k))
+    params = sum(len(c) for c, _h, _s, _seed in reqs)
+
+    def serve(mode):
+        torch_sync()
+        t0 = time.perf_counter()
+        out = qm.batch_serve(reqs, mode=mode, lanes=args.lanes)
+        return out, time.perf_counter() - t0
+
+    for _ in range(max(args.warmup, 3)):
+        serve(qm.BATCH_LANES)
+    barrier(dist, world)
+    with ClockSampler(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
+        times = []
+        for _ in range(args.steps):
+            lanes_out, dt = serve(qm.BATCH_LANES)
+            times.append(dt)
+    wall = max_over_ranks(sum(times), dist, world)
+    plain_out, plain_t = serve(qm.BATCH_PLAIN_LOOP)
+    fused_out, fused_t = serve(qm.BATCH_FUSED_LOOP)
+    gdiff = max(float(np.max(np.abs(np.array(a[1]) - np.array(b[1])))) for a, b in
+                zip(lanes_out, plain_out))
+    ediff = max(abs(a[0] - b[0]) for a, b in zip(lanes_out, plain_out))
+    oracle_err = None
+    if rank == 0:
+        import oracle
+        oracle.build()
+        e_worst = g_worst = g_rel = 0.0
+        checked = 0
+        for (c, _h, _s, _seed), inst, got in zip(reqs, insts, lanes_out):
+            if inst["n"] > 16:
+                continue
+            gates = W.maxcut_qaoa(inst["n"], inst["edges"], inst["gammas"], inst["betas"])
+            e0, g0 = oracle.energy_and_gradient(inst["n"], gates,
+                                                W.maxcut_hamiltonian(inst["edges"]))
+            gd = float(np.max(np.abs(np.array(got[1]) - g0)))
+            e_worst = max(e_worst, abs(got[0] - e0))
+            g_worst = max(g_worst, gd)
+            g_rel = max(g_rel, gd / max(float(np.max(np.abs(g0))), 1e-30))
+            checked += 1
+        oracle_err = {"requests_checked": checked, "widths": "n <= 16",
+                      "max_abs_energy_err": e_worst, "max_abs_grad_err": g_worst,
+                      "max_grad_err_rel_to_max_grad": g_rel}
+    value = world * args.steps * len(reqs) / wall
+    if rank == 0:
+        widths = sorted({i["n"] for i in insts})
+        line = {
+            "metric": "batched_adjoint_requests_per_s", "value": round(value, 2),
+            "unit": "requests/s", "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * wall / args.steps, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "synthetic",
+            "config": {"workload": f"{len(reqs)} QAOA MaxCut requests (energy + adjoint "
+                                   "gradient + 4096 samples each)",
+                       "widths": widths, "gate_params": params, "lanes": args.lanes},
+            "plain_loop": {"value": round(len(reqs) / plain_t, 2), "unit": "requests/s",
+                           "seconds": round(plain_t, 3),
+                           "what": "per-circuit loop: gate-by-gate adjoint, run, sample"},
+            "blockwise_loop": {"value": round(len(reqs) / fused_t, 2), "unit": "requests/s",
+                               "seconds": round(fused_t, 3)},
+            "speedup_vs_plain_loop": round(plain_t / (wall / args.steps), 2),
+            "max_grad_diff_vs_plain": gdiff, "max_energy_diff_vs_plain": ediff,
+            "err_vs_complex128_oracle": oracle_err,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    barrier(dist, world)
+
+
+def run_grad_workload(args, world, rank, dist):
+    """Adjoint gradients of the HEA depth-8 problem (RY + RZ per wire per
+    layer, CX ladder; H = -sum Z_i Z_{i+1} - 0.7 sum X_i on a ring) at 28 and
+    33 qubits: device time per gradient with the block-wise sweep (the
+    default) and with the reference's gate-by-gate sweep, and a central
+    difference check (eps = 1e-3) on a few parameters."""
+    import numpy as np
+    import qmetal_gb300 as qm
+    from qmetal_gb300 import workloads as W
+    results = {}
+    for n in args.grad_qubits:
+        gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
+        c, h = W.to_circuit(n, gates), W.to_hamiltonian(terms)
+        nparams = sum(1 for g in gates if g[2])
+        sim = qm.Simulator(n)
+        entry = {"gates": len(gates), "params": nparams}
+        for label, fused in (("blockwise", True), ("gate_by_gate", False)):
+            sim.energy_and_gradient(c, h, fused=fused)      # warm-up
+            sim.elapsed()
+            reps = args.steps if fused else 1
+            for _ in range(reps):
+                e, g = sim.energy_and_gradient(c, h, fused=fused)
+            t = sim.elapsed() / reps
+            entry[label] = {"s_per_gradient": round(t, 4), "grad_per_s": round(1.0 / t, 3),
+                            "param_grads_per_s": round(nparams / t, 1)}
+            entry.setdefault("energy", e)
+            entry.setdefault("_grad", g)
+        entry["speedup"] = round(entry["gate_by_gate"]["s_per_gradient"]
+                                 / entry["blockwise"]["s_per_gradient"], 2)
+        g = entry.pop("_grad")
+        worst = 0.0
+        eps = 1e-3
+        for j in (0, len(gates) // 2, len(gates) - n - 2):
+            while not gates[j][2]:
+                j += 1
+            kind, qs, ps = gates[j]
+            plus = list(gates); plus[j] = (kind, qs, (ps[0] + eps,))
+            minus = list(gates); minus[j] = (kind, qs, (ps[0] - eps,))
+            sim.reset(); sim.run(W.to_circuit(n, plus)); ep = sim.expectation(h)
+            sim.reset(); sim.run(W.to_circuit(n, minus)); em = sim.expectation(h)
+            worst = max(worst, abs((ep - em) / (2 * eps) - g[j]))
+        entry["max_abs_diff_vs_central_difference"] = worst
+        results[f"n{n}"] = entry
+        sim.close()
+        del sim
+    if rank == 0:
+        first = results[f"n{args.grad_qubits[0]}"]
+        line = {
+            "metric": "adjoint_gradients_per_s", "value": first["blockwise"]["grad_per_s"],
+            "unit": "gradients/s", "n_gpus": world, "steps": args.steps, "warmup": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
+            "data": "synthetic",
+            "config": {"workload": "HEA depth 8 (RY+RZ per wire per layer, CX ladder), ring "
+                                   "TFIM Hamiltonian hx=0.7", "qubits": args.grad_qubits},
+            "results": results,
+        }
+        print(json.dumps(line), flush=True)
+
+
 def main():
+    global N_CPU
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
@@ -245,8 +389,23 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--qubits", type=int, default=N_QUBITS)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-scale", action="store_true",
+                    help="skip the GHZ / QFT runs at 33 and 34 qubits")
+    ap.add_argument("--workload", default="fused30", choices=["fused30", "batch", "grad"])
+    ap.add_argument("--grad-qubits", type=int, nargs="+", default=[28, 33])
+    ap.add_argument("--requests", type=int, default=512)
+    ap.add_argument("--lanes", type=int, default=8)
+    ap.add_argument("--cpu-qubits", type=int, default=N_CPU,
+                    help="width of the bounded CPU sample (reference arm, cpu_baseline)")
     args = ap.parse_args()
     world, rank, local, dist = dist_setup()
+    N_CPU = args.cpu_qubits
+    if args.workload == "batch" and args.impl != "reference":
+        run_batch_workload(args, world, rank, dist)
+        return
+    if args.workload == "grad" and args.impl != "reference":
+        run_grad_workload(args, world, rank, dist)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
         barrier(dist, world)
@@ -328,6 +487,38 @@ def main():
     e2e_wall = max_over_ranks(time.perf_counter() - t0, dist, world)
     e2e_value = world * args.steps * step_bytes / e2e_wall / 1e9
 
+    # --- scale: GHZ and QFT at 33 and 34 qubits (64 / 128 GiB in place) -------
+    scale = {}
+    if not args.no_scale:
+        sim.close()
+        del sim
+        for ns in (33, 34):
+            try:
+                big = qm.Simulator(ns)
+            except qm.QMetalError as e:
+                scale[f"n{ns}"] = {"skipped": str(e)}
+                continue
+            for name, gates in (("ghz", W.ghz(ns)), ("qft", W.qft(ns))):
+                c = W.to_circuit(ns, gates)
+                ks = plan_kinds(c.plan_export())
+                big.reset()
+                big.run(c)
+                big.synchronize()
+                big.elapsed()
+                big.reset()
+                big.run(c)
+                t = big.elapsed()
+                nbytes = circuit_bytes(ks, ns)
+                entry = {"gates": len(gates), "plan_ops": len(ks), "s_per_circuit": round(t, 4),
+                         "gbs": round(nbytes / t / 1e9, 1),
+                         "frac": round(nbytes / t / 1e9 / peaks()[0], 4),
+                         "norm": big.norm(), "z0": big.expectation_pauli(z_mask=1)}
+                if name == "ghz":
+                    entry["z0_zlast"] = big.expectation_pauli(z_mask=1 | (1 << (ns - 1)))
+                scale[f"{name}_{ns}"] = entry
+            big.close()
+            del big
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -363,6 +554,7 @@ def main():
             "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h},
             "gpu_launches": int(launches),
+            "scale": scale,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
             "wall_s_timed": round(wall, 3),

@@ -145,6 +145,33 @@ int qm_elapsed(qm_simulator s, double *out_seconds);
 int qm_run_profiled(qm_simulator s, qm_circuit c, int fuse, double *out_seconds,
                     size_t cap, size_t *out_count);
 
+/* qm_energy_and_gradient with the backward sweep chosen: mode 0 is the
+ * block-wise sweep qm_energy_and_gradient uses (commuting blocks undone in
+ * one pass each), mode 1 the reference's gate-by-gate sweep. */
+int qm_energy_and_gradient_mode(qm_simulator s, qm_circuit c,
+                                const qm_hamiltonian *h, int mode,
+                                double *out_energy, double *out_grad);
+
+/* One serving request of a batch: the circuit's width is its qubit count. */
+typedef struct {
+  qm_circuit circuit;
+  const qm_hamiltonian *hamiltonian;
+  size_t shots;
+  uint64_t seed;
+  double *out_energy;      /* 1 value (may be NULL) */
+  double *out_grad;        /* qm_circuit_size(circuit) values */
+  uint64_t *out_samples;   /* shots values */
+} qm_batch_item;
+
+/* Energy, adjoint gradient and samples for `count` requests of any widths.
+ * mode 0: concurrent lanes (`lanes` host threads, each with its own stream),
+ *         block-wise adjoint, one synchronisation per request;
+ * mode 1: one request after another as a per-circuit caller would run them
+ *         (gate-by-gate adjoint, then run and sample);
+ * mode 2: one request after another with the block-wise adjoint.
+ * Every mode returns the same numbers to within float round-off. */
+int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t lanes);
+
 #ifdef __cplusplus
 }
 #endif

@@ -129,6 +129,40 @@ int qmk_adjoint_1q(float *psi, float *lambda, uint32_t n, uint32_t q,
                    const float minv[8], int generator, double *d_grad,
                    void *workspace, size_t workspace_bytes, void *stream);
 
+/* Co-state of a Hamiltonian of Z strings (each mask at most two bits):
+ * lambda_i = D(i) psi_i with D(i) = sum_t c_t (-1)^{popcount(i & z_t)}, and
+ * *d_energy = sum_i D(i) |psi_i|^2, in one pass. Returns -1 (nothing
+ * launched) if a mask has three or more bits. Replaces the per-term
+ * pauli_accum passes and the host energy loop for such Hamiltonians
+ * (kernels.metal:313-327; simulator.mm:856-904). */
+int qmk_zdiag_costate(float *lambda, const float *psi, uint32_t n, uint32_t num_terms,
+                      const uint64_t *z_masks, const double *coeffs, double *d_energy,
+                      void *workspace, size_t workspace_bytes, void *stream);
+
+/* Backward step over a whole diagonal block (terms as in
+ * qmk_apply_diagonal, describing the block's forward phases): for each of the
+ * ngen <= 32 Z-string generators, d_grad[slots[t]] = Im<lambda|Z_gen|psi>;
+ * then, if undo, both states are multiplied by the conjugate phases, all in
+ * one pass. Replaces the per-gate reduce_pauli2 and undo dispatches for the
+ * block's RZ gates and ZZ couplings (kernels.metal:331-360;
+ * simulator.mm:914-959). */
+int qmk_adjoint_diagonal(float *psi, float *lambda, uint32_t n, uint32_t num_terms,
+                         const uint64_t *masks, const double *angles, double global_phase,
+                         uint32_t ngen, const uint64_t *gen_masks, const uint32_t *slots,
+                         double *d_grad, int undo, void *workspace, size_t workspace_bytes,
+                         void *stream);
+
+/* Backward step over one-qubit gates on at most three wires >= 1 plus wire 0,
+ * applied in the given order (each wire's gates last to first): op o takes
+ * d_grad[slots[o]] = Im<lambda|P|psi> if gens[o] is 1/2/3 (X/Y/Z), then
+ * applies minv[8o..8o+7] to both states; up to 16 ops, one pass. Replaces the
+ * per-gate reduce_pauli2 and undo dispatches (kernels.metal:331-360;
+ * simulator.mm:914-959). */
+int qmk_adjoint_group(float *psi, float *lambda, uint32_t n, uint32_t num_ops,
+                      const uint32_t *wires, const float *minv, const int *gens,
+                      const uint32_t *slots, double *d_grad, void *workspace,
+                      size_t workspace_bytes, void *stream);
+
 /* Sampling workspace bytes for n qubits (block CDF in FP64). */
 size_t qmk_sample_workspace_bytes(uint32_t n);
 

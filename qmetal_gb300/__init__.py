@@ -29,7 +29,7 @@ from ctypes import (
 )
 
 __all__ = ["Circuit", "Simulator", "Hamiltonian", "QMetalError", "version",
-           "is_available", "device_name", "max_qubits", "library_path"]
+           "is_available", "device_name", "max_qubits", "library_path", "batch_serve"]
 
 
 class QMetalError(RuntimeError):
@@ -121,7 +121,18 @@ _expect_terms = _decl("qm_expectation_terms", c_int, c_void_p,
 _sample = _decl("qm_sample", c_int, c_void_p, c_size_t, c_uint64, _u64p)
 _energy_grad = _decl("qm_energy_and_gradient", c_int, c_void_p, c_void_p,
                      POINTER(_Hamiltonian), _f64p, _f64p)
+_energy_grad_mode = _decl("qm_energy_and_gradient_mode", c_int, c_void_p, c_void_p,
+                          POINTER(_Hamiltonian), c_int, _f64p, _f64p)
 _elapsed = _decl("qm_elapsed", c_int, c_void_p, _f64p)
+
+
+class _BatchItem(ctypes.Structure):
+    _fields_ = [("circuit", c_void_p), ("hamiltonian", POINTER(_Hamiltonian)),
+                ("shots", c_size_t), ("seed", c_uint64), ("out_energy", _f64p),
+                ("out_grad", _f64p), ("out_samples", _u64p)]
+
+
+_batch_serve = _decl("qm_batch_serve", c_int, POINTER(_BatchItem), c_size_t, c_int, c_uint32)
 _run_profiled = _decl("qm_run_profiled", c_int, c_void_p, c_void_p, c_int, _f64p,
                       c_size_t, POINTER(c_size_t))
 
@@ -387,12 +398,17 @@ class Simulator:
             out[key] = out.get(key, 0) + 1
         return dict(sorted(out.items(), key=lambda kv: -kv[1]))
 
-    def energy_and_gradient(self, circuit: Circuit, hamiltonian: Hamiltonian):
-        """Adjoint gradient: one entry per gate, zero where unparameterised."""
+    def energy_and_gradient(self, circuit: Circuit, hamiltonian: Hamiltonian,
+                            fused: bool = True):
+        """Adjoint gradient: one entry per gate, zero where unparameterised.
+        fused=False runs the reference's gate-by-gate backward sweep."""
         h = hamiltonian._c()
         energy = c_double()
         grad = (c_double * max(1, len(circuit)))()
-        _check(_energy_grad(self._h, circuit._h, byref(h), byref(energy), grad))
+        if fused:
+            _check(_energy_grad(self._h, circuit._h, byref(h), byref(energy), grad))
+        else:
+            _check(_energy_grad_mode(self._h, circuit._h, byref(h), 1, byref(energy), grad))
         return energy.value, list(grad)[:len(circuit)]
 
     def run_profiled(self, circuit: Circuit, fuse: bool = True):
@@ -409,3 +425,33 @@ class Simulator:
         out = c_double()
         _check(_elapsed(self._h, byref(out)))
         return out.value
+
+
+BATCH_LANES, BATCH_PLAIN_LOOP, BATCH_FUSED_LOOP = 0, 1, 2
+
+
+def batch_serve(requests, mode: int = BATCH_LANES, lanes: int = 8):
+    """Energy, adjoint gradient and samples for many (circuit, hamiltonian,
+    shots, seed) requests of any widths in one call. Returns a list of
+    (energy, gradient list, samples list), in request order."""
+    import numpy as np
+    reqs = list(requests)
+    items = (_BatchItem * max(1, len(reqs)))()
+    keep = []
+    outs = []
+    for i, (circ, ham, shots, seed) in enumerate(reqs):
+        h = ham._c()
+        e = np.zeros(1, dtype=np.float64)
+        g = np.zeros(max(1, len(circ)), dtype=np.float64)
+        s = np.zeros(max(1, int(shots)), dtype=np.uint64)
+        keep.append((h, circ))
+        outs.append((e, g, s, len(circ), int(shots)))
+        items[i].circuit = circ._h
+        items[i].hamiltonian = ctypes.pointer(h)
+        items[i].shots = int(shots)
+        items[i].seed = int(seed)
+        items[i].out_energy = e.ctypes.data_as(_f64p)
+        items[i].out_grad = g.ctypes.data_as(_f64p)
+        items[i].out_samples = s.ctypes.data_as(_u64p)
+    _check(_batch_serve(items, len(reqs), int(mode), int(lanes)))
+    return [(float(e[0]), g[:ng].tolist(), s[:ns].tolist()) for e, g, s, ng, ns in outs]

@@ -30,9 +30,11 @@ CXX = os.environ.get("CXX", "g++")
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextra",
              "-I" + os.path.join(CUDA_HOME, "include")]
 
-CU_SOURCES = ["k_gates.cu", "k_diag.cu", "k_reduce.cu", "k_sample.cu", "k_noalloc.cu"]
-CXX_SOURCES = ["circuit.cpp", "plan.cpp", "simulator.cpp", "capi.cpp"]
-HEADERS = ["kcommon.cuh", "circuit.hpp", "simulator.hpp"]
+CU_SOURCES = ["k_gates.cu", "k_diag.cu", "k_reduce.cu", "k_sample.cu", "k_adjoint.cu",
+              "k_noalloc.cu"]
+CXX_SOURCES = ["circuit.cpp", "plan.cpp", "simulator.cpp", "batch.cpp", "capi.cpp"]
+HEADERS = ["kcommon.cuh", "kquad.cuh", "kreduce.cuh", "circuit.hpp", "simulator.hpp",
+           "batch.hpp"]
 PUBLIC = [os.path.join(ROOT, "include", "qmetal", "qmetal.h"),
           os.path.join(ROOT, "include", "qmetal", "qmetal_kernels.h")]
 
@@ -70,7 +72,8 @@ def build(verbose: bool = False) -> str:
         objs = list(ex.map(_compile, sources))
     if not _newer(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", tmp] + objs + ["-cudart", "static",
+                                                                "-Xcompiler", "-pthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed: {' '.join(cmd)}\n{r.stdout}\n{r.stderr}")

@@ -13,6 +13,7 @@
 #include <string>
 
 #include "circuit.hpp"
+#include "batch.hpp"
 #include "simulator.hpp"
 
 using namespace qmetal;
@@ -379,6 +380,51 @@ int qm_run_profiled(qm_simulator s, qm_circuit c, int fuse, double *out, size_t 
     s->s->run_profiled(build_plan(c->c, fuse ? FusionOptions{} : FusionOptions::none()), t);
     if (out) std::memcpy(out, t.data(), sizeof(double) * std::min(cap, t.size()));
     if (count) *count = t.size();
+  });
+}
+
+int qm_energy_and_gradient_mode(qm_simulator s, qm_circuit c, const qm_hamiltonian *h, int mode,
+                                double *out_energy, double *out_grad) {
+  if (!s || !c || !h || !out_grad) {
+    set_error("null argument");
+    return -1;
+  }
+  if (mode != 0 && mode != 1) {
+    set_error("gradient mode must be 0 (block-wise) or 1 (gate by gate)");
+    return -1;
+  }
+  return guarded([&] {
+    auto r = s->s->energy_and_gradient(c->c, hamiltonian_of(h), mode == 0);
+    if (out_energy) *out_energy = r.first;
+    if (!r.second.empty()) std::memcpy(out_grad, r.second.data(), r.second.size() * sizeof(double));
+  });
+}
+
+int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t lanes) {
+  if (count && !items) {
+    set_error("null argument");
+    return -1;
+  }
+  if (mode < 0 || mode > 2) {
+    set_error("batch mode must be 0, 1 or 2");
+    return -1;
+  }
+  return guarded([&] {
+    std::vector<Hamiltonian> hams(count);
+    std::vector<BatchItem> v(count);
+    for (size_t i = 0; i < count; i++) {
+      if (!items[i].circuit || !items[i].hamiltonian)
+        throw std::runtime_error("batch: null circuit or Hamiltonian");
+      hams[i] = hamiltonian_of(items[i].hamiltonian);
+      v[i].circuit = &items[i].circuit->c;
+      v[i].hamiltonian = &hams[i];
+      v[i].shots = items[i].shots;
+      v[i].seed = items[i].seed;
+      v[i].energy = items[i].out_energy;
+      v[i].grad = items[i].out_grad;
+      v[i].samples = items[i].out_samples;
+    }
+    run_batch(v, static_cast<BatchMode>(mode), lanes);
   });
 }
 

@@ -107,6 +107,14 @@ struct FusionOptions {
 Plan build_plan(const Circuit &c, const FusionOptions &opts = {});
 bool is_diagonal(const Gate &g);
 
+// Diagonal contribution of a gate: appends its (mask, angle) term and returns
+// the global phase it carries (src/plan.cpp:106-135). Precondition:
+// is_diagonal(g).
+double diagonal_term(const Gate &g, std::vector<uint64_t> &masks, std::vector<double> &angles);
+
+// Is c.ops[i..i+2] a CX(a,b) . RZ_b(t) . CX(a,b) coupling (src/plan.cpp:145-157)?
+bool zz_coupling_at(const Circuit &c, size_t i, uint32_t *a, uint32_t *b, double *t);
+
 // Flat serialisation of a plan, all doubles (masks are < 2^53):
 //   [num_ops] then per op: kind, q0, q1, q2, block_bits, n_group, n_terms,
 //   global_phase, matrix[8], group_qubits[n_group], group_matrices[8*n_group],

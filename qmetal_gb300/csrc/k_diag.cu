@@ -22,61 +22,19 @@
 // a direct per-amplitude FP64 kernel.
 #include <algorithm>
 #include <cstring>
-#include <map>
 #include <vector>
 
-#include "kcommon.cuh"
+#include "kquad.cuh"
 #include "../../include/qmetal/qmetal_kernels.h"
 
 using namespace qmk;
 using qmk_host::grid_for;
 using qmk_host::launch_status;
 
-namespace {
-
-constexpr uint32_t kWMax = 13;
-constexpr uint32_t kMaxPairs = 600;  // n <= 34 has at most 561 distinct pairs
-
-struct alignas(16) DiagDesc {
-  uint32_t n, W;
-  uint32_t nlow, ncross, nhigh;     // pair segments, in this order
-  uint32_t coff[kWMax + 1];         // cross pairs of low bit r: nlow+coff[r] ..
-  double g;
-  double a[64];                     // single-bit angles per wire
-  uint16_t pq[kMaxPairs];           // low wire | high wire << 8
-  double pb[kMaxPairs];
-};
-
-// Workspace layout (qmk_workspace_bytes): [desc][TL table][reduction area].
-constexpr size_t kDescBytes = (sizeof(DiagDesc) + 255) & ~size_t(255);
-constexpr size_t kTableBytes = sizeof(float2) << kWMax;
-}  // namespace
-
-// Offsets shared with k_reduce.cu.
+// Offsets shared with the reduction kernels.
 size_t qmk_reduce_area_offset() { return kDescBytes + kTableBytes; }
 
 namespace {
-
-__global__ void k_diag_prep(const DiagDesc d, DiagDesc *__restrict__ out,
-                            float2 *__restrict__ table) {
-  if (blockIdx.x == 0) {
-    const uint64_t *src = reinterpret_cast<const uint64_t *>(&d);
-    uint64_t *dst = reinterpret_cast<uint64_t *>(out);
-    for (uint32_t k = threadIdx.x; k < sizeof(DiagDesc) / 8; k += blockDim.x) dst[k] = src[k];
-  }
-  const uint32_t lo = blockIdx.x * blockDim.x + threadIdx.x;
-  if (lo >= (1u << d.W)) return;
-  double phi = 0.0;
-  for (uint32_t r = 0; r < d.W; r++)
-    if (lo >> r & 1) phi += d.a[r];
-  for (uint32_t p = 0; p < d.nlow; p++) {
-    const uint32_t q = d.pq[p] & 255, r = d.pq[p] >> 8;
-    if ((lo >> q & 1) && (lo >> r & 1)) phi += d.pb[p];
-  }
-  double s, c;
-  sincos(phi, &s, &c);
-  table[lo] = make_float2(static_cast<float>(c), static_cast<float>(s));
-}
 
 __global__ void __launch_bounds__(kThreads)
 k_diag(float4 *__restrict__ st, const DiagDesc *__restrict__ d,
@@ -85,45 +43,13 @@ k_diag(float4 *__restrict__ st, const DiagDesc *__restrict__ d,
   __shared__ float2 eH;
   __shared__ __align__(16) float2 Y1[64];
   __shared__ float2 Y2[1 << (kWMax - 6)];
-  const uint32_t W = d->W, n = d->n;
-  const uint32_t w1 = W < 6 ? W : 6, w2 = W - w1;
+  const uint32_t W = d->W;
   const uint32_t tid = threadIdx.x;
   const uint32_t nv = 1u << (W - 1);
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    if (tid < W) {
-      double c = 0.0;
-      const uint32_t b0 = d->nlow + d->coff[tid], b1 = d->nlow + d->coff[tid + 1];
-      for (uint32_t p = b0; p < b1; p++) {
-        const uint32_t hq = d->pq[p] >> 8;
-        if (tile >> (hq - W) & 1) c += d->pb[p];
-      }
-      f[tid] = expi_reduced(c);
-    } else if (tid >= 32 && tid < 64) {
-      const uint32_t lane = tid - 32;
-      double s = 0.0;
-      for (uint32_t q = W + lane; q < n; q += 32)
-        if (tile >> (q - W) & 1) s += d->a[q];
-      const uint32_t p0 = d->nlow + d->ncross, p1 = p0 + d->nhigh;
-      for (uint32_t p = p0 + lane; p < p1; p += 32) {
-        const uint32_t q = d->pq[p] & 255, r = d->pq[p] >> 8;
-        if ((tile >> (q - W) & 1) && (tile >> (r - W) & 1)) s += d->pb[p];
-      }
-      s = warp_sum(s);
-      if (lane == 0) eH = expi_reduced(d->g + s);
-    }
+    tile_coeffs<true>(d, tile, f, &eH, nullptr, nullptr, false);
     __syncthreads();
-    if (tid < (1u << w1)) {
-      float2 y = make_float2(1.0f, 0.0f);
-      for (uint32_t r = 0; r < w1; r++)
-        if (tid >> r & 1) y = cmul(y, f[r]);
-      Y1[tid] = y;
-    } else if (tid >= 64 && tid - 64 < (1u << w2)) {
-      const uint32_t e = tid - 64;
-      float2 y = eH;
-      for (uint32_t r = 0; r < w2; r++)
-        if (e >> r & 1) y = cmul(y, f[w1 + r]);
-      Y2[e] = y;
-    }
+    tile_phase_tables(W, f, eH, Y1, Y2);
     __syncthreads();
     const uint64_t base = tile << (W - 1);
     constexpr int UU = 4;
@@ -193,56 +119,14 @@ extern "C" int qmk_apply_diagonal(float *state, uint32_t n, uint32_t nt,
   cudaStream_t s = (cudaStream_t)stream;
   const uint32_t W = std::min<uint32_t>(n, kWMax);
   DiagDesc d;
-  std::memset(&d, 0, sizeof(d));
-  d.n = n;
-  d.W = W;
-  d.g = global_phase;
-  std::map<std::pair<uint32_t, uint32_t>, double> pairs;
   std::vector<uint64_t> gm;
   std::vector<double> ga;
-  for (uint32_t t = 0; t < nt; t++) {
-    const uint64_t m = masks[t];
-    if (n < 64 && (m >> n)) return -1;
-    const int pc = __builtin_popcountll(m);
-    if (pc == 0) {
-      d.g += angles[t];
-    } else if (pc == 1) {
-      d.a[__builtin_ctzll(m)] += angles[t];
-    } else if (pc == 2) {
-      const uint32_t q = __builtin_ctzll(m), r = 63 - __builtin_clzll(m);
-      pairs[{q, r}] += angles[t];
-    } else {
-      gm.push_back(m);
-      ga.push_back(angles[t]);
-    }
-  }
-  if (pairs.size() > kMaxPairs) return -1;
-  std::vector<std::pair<uint32_t, double>> low, high;
-  std::vector<std::vector<std::pair<uint32_t, double>>> cross(W);
-  for (const auto &kv : pairs) {
-    const uint32_t q = kv.first.first, r = kv.first.second;
-    const uint32_t packed = q | (r << 8);
-    if (r < W) low.push_back({packed, kv.second});
-    else if (q < W) cross[q].push_back({packed, kv.second});
-    else high.push_back({packed, kv.second});
-  }
-  uint32_t p = 0;
-  for (auto &e : low) { d.pq[p] = uint16_t(e.first); d.pb[p] = e.second; p++; }
-  d.nlow = p;
-  for (uint32_t r = 0; r < W; r++) {
-    d.coff[r] = p - d.nlow;
-    for (auto &e : cross[r]) { d.pq[p] = uint16_t(e.first); d.pb[p] = e.second; p++; }
-  }
-  d.coff[W] = p - d.nlow;
-  for (uint32_t r = W + 1; r <= kWMax; r++) d.coff[r] = d.coff[W];
-  d.ncross = p - d.nlow;
-  for (auto &e : high) { d.pq[p] = uint16_t(e.first); d.pb[p] = e.second; p++; }
-  d.nhigh = p - d.nlow - d.ncross;
+  if (build_quad_desc(n, nt, masks, angles, global_phase, d, &gm, &ga) != 0) return -1;
 
   uint8_t *base = static_cast<uint8_t *>(ws);
   DiagDesc *dd = reinterpret_cast<DiagDesc *>(base);
   float2 *table = reinterpret_cast<float2 *>(base + kDescBytes);
-  k_diag_prep<<<grid_for(1u << W, kThreads), kThreads, 0, s>>>(d, dd, table);
+  k_quad_prep<true><<<grid_for(1u << W, kThreads), kThreads, 0, s>>>(d, dd, table);
   int rc = launch_status();
   if (rc) return rc;
   const uint64_t ntiles = 1ull << (n - W);

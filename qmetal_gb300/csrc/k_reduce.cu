@@ -8,69 +8,16 @@
 #include <algorithm>
 #include <cstring>
 
-#include "kcommon.cuh"
+#include "kreduce.cuh"
 #include "../../include/qmetal/qmetal_kernels.h"
 
 using namespace qmk;
 using qmk_host::grid_for;
 using qmk_host::launch_status;
 
-size_t qmk_reduce_area_offset();  // k_diag.cu
-
 namespace {
 
 constexpr int kMaxT = 16;
-constexpr uint32_t kMaxBlocks = 1024;
-
-struct Area {
-  double *partials;   // kMaxBlocks x 32
-  unsigned *counter;
-};
-
-Area area_of(void *ws) {
-  uint8_t *b = static_cast<uint8_t *>(ws) + qmk_reduce_area_offset();
-  Area a;
-  a.partials = reinterpret_cast<double *>(b);
-  a.counter = reinterpret_cast<unsigned *>(b + kMaxBlocks * 32 * sizeof(double));
-  return a;
-}
-
-unsigned reduce_grid() {
-  return std::min<unsigned>(kMaxBlocks, static_cast<unsigned>(qmk_host::num_sms()) * 4);
-}
-
-// Block-reduce acc[0..T) (FP64), then the last block sums the per-block
-// partials in order into out[t] (or adds into out[t] when `add`).
-template <int T>
-__device__ __forceinline__ void finish(double (&acc)[T], int nt, Area a,
-                                       double *out, bool add) {
-  __shared__ double red[kThreads / 32][T];
-  __shared__ unsigned ticket;
-  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
-#pragma unroll
-  for (int t = 0; t < T; t++) {
-    const double v = warp_sum(acc[t]);
-    if (l == 0) red[w][t] = v;
-  }
-  __syncthreads();
-  if (threadIdx.x < static_cast<unsigned>(nt)) {
-    double s = 0.0;
-    for (int k = 0; k < kThreads / 32; k++) s += red[k][threadIdx.x];
-    a.partials[blockIdx.x * 32 + threadIdx.x] = s;
-  }
-  __threadfence();
-  __syncthreads();
-  if (threadIdx.x == 0) ticket = atomicAdd(a.counter, 1u);
-  __syncthreads();
-  if (ticket != gridDim.x - 1) return;
-  __threadfence();
-  if (threadIdx.x < static_cast<unsigned>(nt)) {
-    double s = 0.0;
-    for (unsigned b = 0; b < gridDim.x; b++) s += __ldcg(&a.partials[b * 32 + threadIdx.x]);
-    out[threadIdx.x] = add ? out[threadIdx.x] + s : s;
-  }
-  if (threadIdx.x == 0) *a.counter = 0u;
-}
 
 constexpr int kChunk = 4;  // vectors per FP32 run and per thread iteration
 
@@ -92,7 +39,7 @@ k_abs2(const float4 *__restrict__ st, uint64_t nvec, Area a, double *out) {
       s = fmaf(x[k].x, x[k].x, fmaf(x[k].y, x[k].y, fmaf(x[k].z, x[k].z, fmaf(x[k].w, x[k].w, s))));
     acc[0] += s;
   }
-  finish<1>(acc, 1, a, out, false);
+  finish<1>(acc, 1, a, OutContig{out, false});
 }
 
 __global__ void __launch_bounds__(kThreads)
@@ -115,7 +62,7 @@ k_dot_re(const float4 *__restrict__ x4, const float4 *__restrict__ y4, uint64_t 
       s = fmaf(x[k].x, y[k].x, fmaf(x[k].y, y[k].y, fmaf(x[k].z, y[k].z, fmaf(x[k].w, y[k].w, s))));
     acc[0] += s;
   }
-  finish<1>(acc, 1, a, out, false);
+  finish<1>(acc, 1, a, OutContig{out, false});
 }
 
 struct PauliArgs {
@@ -156,7 +103,7 @@ k_pauli_z(const float4 *__restrict__ st, uint64_t nvec, PauliArgs p, Area a, dou
 #pragma unroll
     for (int t = 0; t < T; t++) acc[t] += part[t];
   }
-  finish<T>(acc, p.nt, a, out, false);
+  finish<T>(acc, p.nt, a, OutContig{out, false});
 }
 
 // flip != 0: over pairs (i, j = i ^ flip) with bit hbit of i clear,
@@ -190,7 +137,7 @@ k_pauli_x(const float2 *__restrict__ st, uint64_t npairs, PauliArgs p, Area a, d
 #pragma unroll
     for (int t = 0; t < T; t++) acc[t] += part[t];
   }
-  finish<T>(acc, p.nt, a, out, false);
+  finish<T>(acc, p.nt, a, OutContig{out, false});
 }
 
 struct AccumArgs {
@@ -280,7 +227,7 @@ k_adj1q(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsites, uin
     }
     acc[0] += part;
   }
-  if (GEN) finish<1>(acc, 1, a, out, false);
+  if (GEN) finish<1>(acc, 1, a, OutContig{out, false});
 }
 
 template <int T>

@@ -1,0 +1,82 @@
+// kreduce.cuh -- the deterministic device-wide reduction used by every
+// kernel that returns numbers (norms, expectations, energies, gradients).
+//
+// Each block reduces its FP64 accumulators (warp shuffles, then shared
+// memory) into per-block partials in the workspace; the last block to finish
+// (atomic ticket) sums the partials in block order and hands each total to an
+// output functor. A result depends only on the grid size, never on timing.
+#pragma once
+
+#include <algorithm>
+
+#include "kcommon.cuh"
+
+size_t qmk_reduce_area_offset();  // k_diag.cu
+
+namespace qmk {
+
+constexpr uint32_t kMaxBlocks = 1024;
+
+struct Area {
+  double *partials;   // kMaxBlocks x 32
+  unsigned *counter;
+};
+
+inline Area area_of(void *ws) {
+  uint8_t *b = static_cast<uint8_t *>(ws) + qmk_reduce_area_offset();
+  Area a;
+  a.partials = reinterpret_cast<double *>(b);
+  a.counter = reinterpret_cast<unsigned *>(b + kMaxBlocks * 32 * sizeof(double));
+  return a;
+}
+
+inline unsigned reduce_grid() {
+  return std::min<unsigned>(kMaxBlocks, static_cast<unsigned>(qmk_host::num_sms()) * 4);
+}
+
+// out[t] = s (or out[t] += s).
+struct OutContig {
+  double *p;
+  bool add;
+  __device__ void operator()(int t, double s) const { p[t] = add ? p[t] + s : s; }
+};
+
+// out[slot[t]] = s: results scattered to their gate's gradient entry.
+template <int T>
+struct OutSlots {
+  double *p;
+  uint32_t slot[T];
+  __device__ void operator()(int t, double s) const { p[slot[t]] = s; }
+};
+
+template <int T, typename Out>
+__device__ __forceinline__ void finish(double (&acc)[T], int nt, Area a, const Out &out) {
+  __shared__ double red[kThreads / 32][T > 0 ? T : 1];
+  __shared__ unsigned ticket;
+  const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+#pragma unroll
+  for (int t = 0; t < T; t++) {
+    const double v = warp_sum(acc[t]);
+    if (l == 0) red[w][t] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < static_cast<unsigned>(nt)) {
+    double s = 0.0;
+    for (int k = 0; k < kThreads / 32; k++) s += red[k][threadIdx.x];
+    a.partials[blockIdx.x * 32 + threadIdx.x] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) ticket = atomicAdd(a.counter, 1u);
+  __syncthreads();
+  if (ticket != gridDim.x - 1) return;
+  __threadfence();
+  if (threadIdx.x < static_cast<unsigned>(nt)) {
+    double s = 0.0;
+    for (unsigned b = 0; b < gridDim.x; b++) s += __ldcg(&a.partials[b * 32 + threadIdx.x]);
+    out(static_cast<int>(threadIdx.x), s);
+  }
+  if (threadIdx.x == 0) *a.counter = 0u;
+}
+
+}  // namespace qmk

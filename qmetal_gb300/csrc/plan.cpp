@@ -54,39 +54,12 @@ PlanOp dense_op(uint32_t q, const cdouble *m) {
   return op;
 }
 
-// Appends the (mask, angle) term of one diagonal gate; returns its global
-// phase (only RZ has one: RZ(t) = e^{-it/2} diag(1, e^{it})).
 double add_diagonal_term(const Gate &g, PlanOp &op) {
-  const uint64_t b0 = 1ull << g.qubits[0];
-  auto term = [&](uint64_t m, double a) {
-    op.masks.push_back(m);
-    op.angles.push_back(a);
-  };
-  switch (g.kind) {
-    case G_Z: term(b0, M_PI); return 0.0;
-    case G_S: term(b0, M_PI / 2); return 0.0;
-    case G_SDG: term(b0, -M_PI / 2); return 0.0;
-    case G_T: term(b0, M_PI / 4); return 0.0;
-    case G_TDG: term(b0, -M_PI / 4); return 0.0;
-    case G_P: term(b0, g.params[0]); return 0.0;
-    case G_RZ: term(b0, g.params[0]); return -g.params[0] / 2.0;
-    case G_CZ: term(b0 | (1ull << g.qubits[1]), M_PI); return 0.0;
-    case G_CP: term(b0 | (1ull << g.qubits[1]), g.params[0]); return 0.0;
-    default: throw std::runtime_error("diagonal_term: gate is not diagonal");
-  }
+  return diagonal_term(g, op.masks, op.angles);
 }
 
-// CX(a,b) RZ_b(t) CX(a,b) starting at position i?
 bool zz_at(const Circuit &c, size_t i, uint32_t *a, uint32_t *b, double *t) {
-  if (i + 2 >= c.ops.size()) return false;
-  const Gate &x = c.ops[i], &r = c.ops[i + 1], &y = c.ops[i + 2];
-  if (x.kind != G_CX || y.kind != G_CX || r.kind != G_RZ) return false;
-  if (x.qubits[0] != y.qubits[0] || x.qubits[1] != y.qubits[1]) return false;
-  if (r.qubits[0] != x.qubits[1]) return false;
-  *a = x.qubits[0];
-  *b = x.qubits[1];
-  *t = r.params[0];
-  return true;
+  return zz_coupling_at(c, i, a, b, t);
 }
 
 size_t block_at(const Circuit &c, size_t i, bool zz) {
@@ -219,6 +192,41 @@ Plan block_pass(Plan &&in, uint32_t bits) {
 }
 
 }  // namespace
+
+// One diagonal gate's term; RZ(t) = e^{-it/2} diag(1, e^{it}) carries the
+// only global phase.
+double diagonal_term(const Gate &g, std::vector<uint64_t> &masks, std::vector<double> &angles) {
+  const uint64_t b0 = 1ull << g.qubits[0];
+  auto term = [&](uint64_t m, double a) {
+    masks.push_back(m);
+    angles.push_back(a);
+  };
+  switch (g.kind) {
+    case G_Z: term(b0, M_PI); return 0.0;
+    case G_S: term(b0, M_PI / 2); return 0.0;
+    case G_SDG: term(b0, -M_PI / 2); return 0.0;
+    case G_T: term(b0, M_PI / 4); return 0.0;
+    case G_TDG: term(b0, -M_PI / 4); return 0.0;
+    case G_P: term(b0, g.params[0]); return 0.0;
+    case G_RZ: term(b0, g.params[0]); return -g.params[0] / 2.0;
+    case G_CZ: term(b0 | (1ull << g.qubits[1]), M_PI); return 0.0;
+    case G_CP: term(b0 | (1ull << g.qubits[1]), g.params[0]); return 0.0;
+    default: throw std::runtime_error("diagonal_term: gate is not diagonal");
+  }
+}
+
+bool zz_coupling_at(const Circuit &c, size_t i, uint32_t *a, uint32_t *b, double *t) {
+  if (i + 2 >= c.ops.size()) return false;
+  const Gate &x = c.ops[i], &r = c.ops[i + 1], &y = c.ops[i + 2];
+  if (x.kind != G_CX || y.kind != G_CX || r.kind != G_RZ) return false;
+  if (x.qubits[0] != y.qubits[0] || x.qubits[1] != y.qubits[1]) return false;
+  if (r.qubits[0] != x.qubits[1]) return false;
+  *a = x.qubits[0];
+  *b = x.qubits[1];
+  *t = r.params[0];
+  return true;
+}
+
 
 bool is_diagonal(const Gate &g) {
   switch (g.kind) {

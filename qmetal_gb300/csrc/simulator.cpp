@@ -556,10 +556,8 @@ void Simulator::expectation_terms(const Hamiltonian &h, double *out) {
 // ---------------------------------------------------------------------------
 // Sampling
 
-std::vector<uint64_t> Simulator::sample(size_t shots, uint64_t seed) {
-  std::vector<uint64_t> out;
-  if (shots == 0) return out;
-  activate();
+// Queue the sampler; the draws land in d_shots_.
+void Simulator::launch_sample(size_t shots, uint64_t seed) {
   const size_t need = qmk_sample_workspace_bytes(n_);
   if (!sample_ws_) {
     cuda_check(cudaMalloc(&sample_ws_, need), "sampling workspace");
@@ -576,6 +574,13 @@ std::vector<uint64_t> Simulator::sample(size_t shots, uint64_t seed) {
         "sample");
   const uint64_t nb = ((uint64_t(1) << n_) + 1023) / 1024;
   dispatches_ += (nb > 2048) ? 5 : 3;
+}
+
+std::vector<uint64_t> Simulator::sample(size_t shots, uint64_t seed) {
+  std::vector<uint64_t> out;
+  if (shots == 0) return out;
+  activate();
+  launch_sample(shots, seed);
   out.resize(shots);
   cuda_check(cudaMemcpyAsync(out.data(), d_shots_, shots * sizeof(uint64_t),
                              cudaMemcpyDeviceToHost, S(stream_)),
@@ -612,14 +617,15 @@ void Simulator::costate(const Hamiltonian &h) {
   if (first) cuda_check(cudaMemsetAsync(costate_, 0, dim() * 8, S(stream_)), "co-state zero");
 }
 
-std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circuit &c,
-                                                                      const Hamiltonian &h) {
+void Simulator::prepare_adjoint(const Circuit &c, const Hamiltonian &h) {
   if (c.num_qubits != n_) throw std::runtime_error("circuit/simulator size mismatch");
   for (const Gate &g : c.ops) {
     if (g.num_params > 0 && !generator_of(g))
       throw std::runtime_error(std::string("gradient: ") + gate_name(g.kind) +
                                " carries a parameter but has no native generator; only rx, ry "
                                "and rz are differentiable");
+    for (int k = 0; k < g.num_qubits; k++)
+      if (g.qubits[k] >= n_) throw std::runtime_error("qubit index out of range");
   }
   for (const PauliTerm &t : h.terms)
     if (!t.pauli.valid(n_)) throw std::runtime_error("gradient: invalid Pauli term");
@@ -630,56 +636,305 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
     if (dim() * 8 > free_b) throw std::runtime_error("gradient: co-state does not fit on the device");
     cuda_check(cudaMalloc(&costate_, dim() * 8), "gradient: co-state allocation failed");
   }
-  const size_t G = c.ops.size();
-  if (d_grad_cap_ < std::max<size_t>(G, 1)) {
+  const size_t G = std::max<size_t>(c.ops.size(), 1);
+  if (d_grad_cap_ < G) {
     cudaFree(d_grad_);
     d_grad_ = nullptr;
     d_grad_cap_ = 0;
-    cuda_check(cudaMalloc(&d_grad_, std::max<size_t>(G, 1) * sizeof(double)), "gradient buffer");
-    d_grad_cap_ = std::max<size_t>(G, 1);
+    cuda_check(cudaMalloc(&d_grad_, G * sizeof(double)), "gradient buffer");
+    d_grad_cap_ = G;
   }
-  double *d_grad = d_grad_;
+  cuda_check(cudaMemsetAsync(d_grad_, 0, G * sizeof(double), S(stream_)), "gradient zero");
+}
+
+// lambda = H psi and E = <psi|H|psi> into d_results_[0]. A Hamiltonian of Z
+// strings of weight <= 2 takes one fused pass; anything else goes term group
+// by term group, then a dot product.
+double Simulator::energy_and_costate(const Hamiltonian &h) {
+  bool zonly = !h.terms.empty();
+  std::vector<uint64_t> zm;
+  std::vector<double> zc;
+  for (const PauliTerm &t : h.terms) {
+    if (t.pauli.x_mask | t.pauli.y_mask || popc(t.pauli.z_mask) > 2) zonly = false;
+    zm.push_back(t.pauli.z_mask);
+    zc.push_back(t.coefficient);
+  }
+  if (zonly) {
+    check(qmk_zdiag_costate(costate_, state_, n_, static_cast<uint32_t>(zm.size()), zm.data(),
+                            zc.data(), d_results_, ws_, ws_bytes_, stream_),
+          "co-state");
+    dispatches_ += 2;
+  } else {
+    costate(h);
+    check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
+    dispatches_++;
+  }
+  return 0.0;
+}
+
+// The reference's sweep (src/metal/simulator.mm:910-960), one gate at a time:
+// a fused overlap-and-undo pass per one-qubit gate, both states undone for
+// the others.
+void Simulator::sweep_gate_by_gate(const Circuit &c) {
+  for (size_t k = c.ops.size(); k-- > 0;) {
+    const Gate &g = c.ops[k];
+    const Gate inv = invert(g);
+    if (g.num_qubits == 1) {
+      cdouble m[4];
+      gate_matrix_1q(inv.kind, inv.params, m);
+      float f[8];
+      narrow(m, f);
+      const int gen = g.num_params > 0 ? generator_of(g) : 0;
+      check(qmk_adjoint_1q(state_, costate_, n_, g.qubits[0], f, gen, d_grad_ + k, ws_, ws_bytes_,
+                           stream_),
+            "adjoint step");
+      dispatches_++;
+    } else {
+      apply_gate_to(state_, inv);
+      apply_gate_to(costate_, inv);
+    }
+  }
+}
+
+namespace {
+
+// A run of the circuit that the fused sweep undoes as a unit.
+struct Segment {
+  enum Kind { Window, Diag, Single } kind = Single;
+  size_t begin = 0, end = 0;
+  bool has_param = false;
+  // Diag: the block's forward phase terms and its Z-string generators.
+  std::vector<uint64_t> masks;
+  std::vector<double> angles;
+  double gphase = 0.0;
+  std::vector<uint64_t> gens;
+  std::vector<uint32_t> slots;
+};
+
+// Forward segmentation: a maximal run of one-qubit gates is a window; a run
+// of ZZ couplings (CX.RZ.CX) and two-qubit diagonal gates is a diagonal block;
+// anything else stands alone.
+std::vector<Segment> segment_circuit(const Circuit &c) {
+  std::vector<Segment> segs;
+  const size_t G = c.ops.size();
+  size_t i = 0;
+  while (i < G) {
+    const Gate &g = c.ops[i];
+    Segment s;
+    s.begin = i;
+    uint32_t a, b;
+    double t;
+    if (g.num_qubits == 1) {
+      s.kind = Segment::Window;
+      size_t j = i;
+      for (; j < G && c.ops[j].num_qubits == 1; j++)
+        if (c.ops[j].num_params) s.has_param = true;
+      s.end = j;
+    } else if (zz_coupling_at(c, i, &a, &b, &t) || (g.num_qubits == 2 && is_diagonal(g))) {
+      s.kind = Segment::Diag;
+      size_t j = i;
+      while (j < G) {
+        if (zz_coupling_at(c, j, &a, &b, &t)) {
+          const uint64_t ma = 1ull << a, mb = 1ull << b;
+          s.masks.insert(s.masks.end(), {ma, mb, ma | mb});
+          s.angles.insert(s.angles.end(), {t, t, -2.0 * t});
+          s.gphase += -t / 2.0;
+          if (c.ops[j + 1].num_params) {
+            s.gens.push_back(ma | mb);   // exp(-i t/2 Z_a Z_b)
+            s.slots.push_back(static_cast<uint32_t>(j + 1));
+            s.has_param = true;
+          }
+          j += 3;
+        } else if (c.ops[j].num_qubits == 2 && is_diagonal(c.ops[j])) {
+          s.gphase += diagonal_term(c.ops[j], s.masks, s.angles);
+          if (c.ops[j].num_params) s.has_param = true;
+          j++;
+        } else {
+          break;
+        }
+      }
+      s.end = j;
+    } else {
+      s.kind = Segment::Single;
+      s.end = i + 1;
+      s.has_param = g.num_params > 0;
+    }
+    i = s.end;
+    segs.push_back(std::move(s));
+  }
+  return segs;
+}
+
+struct WireOp {
+  uint32_t wire;
+  float minv[8];
+  int gen;
+  uint32_t slot;
+};
+
+}  // namespace
+
+// Block-wise sweep: every gradient of a commuting block is read at the block
+// boundary and the block is undone on both states in the same pass. Blocks
+// before the first parameterised one are never undone.
+void Simulator::sweep_fused(const Circuit &c) {
+  const auto segs = segment_circuit(c);
+  size_t first = segs.size();
+  for (size_t s = 0; s < segs.size(); s++)
+    if (segs[s].has_param) {
+      first = s;
+      break;
+    }
+  constexpr uint32_t kOps = 16, kDiagGens = 32;
+  for (size_t s = segs.size(); s-- > first;) {
+    const Segment &seg = segs[s];
+    const bool undo = s > first;
+    if (seg.kind == Segment::Single) {
+      if (undo) {
+        const Gate inv = invert(c.ops[seg.begin]);
+        apply_gate_to(state_, inv);
+        apply_gate_to(costate_, inv);
+      }
+      continue;
+    }
+    if (seg.kind == Segment::Diag) {
+      const uint32_t ng = static_cast<uint32_t>(seg.gens.size());
+      if (ng == 0 && !undo) continue;
+      uint32_t done = 0;
+      do {
+        const uint32_t take = std::min(kDiagGens, ng - done);
+        const bool last = done + take == ng;
+        check(qmk_adjoint_diagonal(state_, costate_, n_, static_cast<uint32_t>(seg.masks.size()),
+                                   seg.masks.data(), seg.angles.data(), seg.gphase, take,
+                                   take ? &seg.gens[done] : nullptr,
+                                   take ? &seg.slots[done] : nullptr, d_grad_,
+                                   (last && undo) ? 1 : 0, ws_, ws_bytes_, stream_),
+              "adjoint diagonal block");
+        dispatches_ += 2;
+        done += take;
+      } while (done < ng);
+      continue;
+    }
+    // Window: each wire's gates last to first, a few wires per pass.
+    std::vector<std::vector<size_t>> per_wire(n_);
+    for (size_t k = seg.begin; k < seg.end; k++) per_wire[c.ops[k].qubits[0]].push_back(k);
+    std::vector<WireOp> tile;
+    uint32_t others = 0, grads = 0;
+    bool tile_has_param = false;
+    auto flush = [&]() {
+      if (tile.empty()) return;
+      if (undo || tile_has_param) {
+        std::vector<uint32_t> wires, slots;
+        std::vector<float> mats;
+        std::vector<int> gens;
+        for (const WireOp &o : tile) {
+          wires.push_back(o.wire);
+          mats.insert(mats.end(), o.minv, o.minv + 8);
+          gens.push_back(o.gen);
+          slots.push_back(o.slot);
+        }
+        check(qmk_adjoint_group(state_, costate_, n_, static_cast<uint32_t>(tile.size()),
+                                wires.data(), mats.data(), gens.data(), slots.data(), d_grad_, ws_,
+                                ws_bytes_, stream_),
+              "adjoint window");
+        dispatches_++;
+      }
+      tile.clear();
+      others = grads = 0;
+      tile_has_param = false;
+    };
+    for (uint32_t w = 0; w < n_; w++) {
+      if (per_wire[w].empty()) continue;
+      std::vector<WireOp> ops;
+      uint32_t wgrads = 0;
+      for (size_t r = per_wire[w].size(); r-- > 0;) {
+        const size_t k = per_wire[w][r];
+        const Gate &g = c.ops[k];
+        const Gate inv = invert(g);
+        WireOp o{};
+        o.wire = w;
+        cdouble m[4];
+        gate_matrix_1q(inv.kind, inv.params, m);
+        narrow(m, o.minv);
+        o.gen = g.num_params > 0 ? generator_of(g) : 0;
+        o.slot = static_cast<uint32_t>(k);
+        if (o.gen) wgrads++;
+        ops.push_back(o);
+      }
+      const uint32_t need_other = w != 0 ? 1u : 0u;
+      if (ops.size() > kOps) {
+        flush();
+        for (size_t b = 0; b < ops.size(); b += kOps) {
+          const size_t e = std::min(ops.size(), b + kOps);
+          tile.assign(ops.begin() + b, ops.begin() + e);
+          for (const WireOp &o : tile) tile_has_param |= o.gen != 0;
+          flush();
+        }
+        continue;
+      }
+      const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;
+      if (tile.size() + ops.size() > kOps || others + need_other > 3 || grads + wgrads > cap)
+        flush();
+      tile.insert(tile.end(), ops.begin(), ops.end());
+      others += need_other;
+      grads += wgrads;
+      tile_has_param |= wgrads > 0;
+    }
+    flush();
+  }
+}
+
+std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circuit &c,
+                                                                      const Hamiltonian &h,
+                                                                      bool fused) {
+  prepare_adjoint(c, h);
+  const size_t G = c.ops.size();
   std::vector<double> grad(G, 0.0);
-  double energy = 0.0;
   try {
-    cuda_check(cudaMemsetAsync(d_grad, 0, std::max<size_t>(G, 1) * sizeof(double), S(stream_)),
-               "gradient zero");
     // Forward: the fused plan reaches the same final state as the gate
     // stream; only the backward sweep needs per-gate identity.
     reset();
     run(build_plan(c, FusionOptions{}));
-    costate(h);
-    check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
-    dispatches_++;
-    for (size_t k = G; k-- > 0;) {
-      const Gate &g = c.ops[k];
-      const Gate inv = invert(g);
-      if (g.num_qubits == 1) {
-        if (g.qubits[0] >= n_) throw std::runtime_error("qubit index out of range");
-        cdouble m[4];
-        gate_matrix_1q(inv.kind, inv.params, m);
-        float f[8];
-        narrow(m, f);
-        const int gen = g.num_params > 0 ? generator_of(g) : 0;
-        check(qmk_adjoint_1q(state_, costate_, n_, g.qubits[0], f, gen, d_grad + k, ws_, ws_bytes_,
-                             stream_),
-              "adjoint step");
-        dispatches_++;
-      } else {
-        apply_gate_to(state_, inv);
-        apply_gate_to(costate_, inv);
-      }
-    }
-    cuda_check(cudaMemcpyAsync(grad.data(), d_grad, G * sizeof(double), cudaMemcpyDeviceToHost,
-                               S(stream_)),
-               "gradient copy");
+    energy_and_costate(h);
+    if (fused) sweep_fused(c);
+    else sweep_gate_by_gate(c);
+    if (G)
+      cuda_check(cudaMemcpyAsync(grad.data(), d_grad_, G * sizeof(double), cudaMemcpyDeviceToHost,
+                                 S(stream_)),
+                 "gradient copy");
     fetch(1);
-    energy = h_results_[0];
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
     throw;
   }
-  return {energy, grad};
+  return {h_results_[0], grad};
+}
+
+// One serving request: forward once, draw the samples from the final state,
+// then energy and the block-wise adjoint gradient; one synchronisation.
+void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint64_t seed,
+                      double *energy, double *grad, uint64_t *samples) {
+  prepare_adjoint(c, h);
+  try {
+    reset();
+    run(build_plan(c, FusionOptions{}));
+    if (shots) launch_sample(shots, seed);
+    energy_and_costate(h);
+    sweep_fused(c);
+    if (!c.ops.empty() && grad)
+      cuda_check(cudaMemcpyAsync(grad, d_grad_, c.ops.size() * sizeof(double),
+                                 cudaMemcpyDeviceToHost, S(stream_)),
+                 "gradient copy");
+    if (shots && samples)
+      cuda_check(cudaMemcpyAsync(samples, d_shots_, shots * sizeof(uint64_t),
+                                 cudaMemcpyDeviceToHost, S(stream_)),
+                 "sample copy");
+    fetch(1);
+  } catch (...) {
+    cudaStreamSynchronize(S(stream_));
+    throw;
+  }
+  if (energy) *energy = h_results_[0];
 }
 
 double Simulator::elapsed() {

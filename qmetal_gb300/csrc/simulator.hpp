@@ -50,8 +50,17 @@ class Simulator {
 
   std::vector<uint64_t> sample(size_t shots, uint64_t seed = 0);
 
+  // Adjoint energy and per-gate gradient. fused = true runs the block-wise
+  // backward sweep (commuting blocks undone in one pass each); false runs the
+  // reference's gate-by-gate sweep.
   std::pair<double, std::vector<double>> energy_and_gradient(const Circuit &c,
-                                                             const Hamiltonian &h);
+                                                             const Hamiltonian &h,
+                                                             bool fused = true);
+
+  // Forward, samples from the final state, energy and block-wise gradient in
+  // one queued sequence with a single synchronisation.
+  void serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint64_t seed, double *energy,
+             double *grad, uint64_t *samples);
 
   uint64_t dispatch_count() const { return dispatches_; }
   double elapsed();
@@ -69,7 +78,12 @@ class Simulator {
   void apply_op_to(float *state, const PlanOp &op);
   void pauli_values(const float *state, const Hamiltonian &h, std::vector<double> &vals);
   void costate(const Hamiltonian &h);
+  void prepare_adjoint(const Circuit &c, const Hamiltonian &h);
+  double energy_and_costate(const Hamiltonian &h);
+  void sweep_gate_by_gate(const Circuit &c);
+  void sweep_fused(const Circuit &c);
   void fetch(size_t count);             // d_results_ -> h_results_, sync
+  void launch_sample(size_t shots, uint64_t seed);
 
   uint32_t n_ = 0;
   int device_ = 0;

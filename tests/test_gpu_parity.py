@@ -380,6 +380,62 @@ def test_gradient_closed_form_and_fail_closed():
         qm.Simulator(2).energy_and_gradient(bad, qm.Hamiltonian().add_string(1.0, "ZI"))
 
 
+def _fused_cases():
+    rng = np.random.default_rng(77)
+    n = 11
+    zz_many = [(H, (q,), ()) for q in range(n)]
+    for _ in range(40):                     # 40 couplings in one block: > 32 generators
+        a, b = (int(x) for x in rng.choice(n, size=2, replace=False))
+        zz_many += [(CX, (a, b), ()), (RZ, (b,), (float(rng.uniform(-2, 2)),)), (CX, (a, b), ())]
+    zz_many += [(RX, (q,), (float(rng.uniform(-2, 2)),)) for q in range(n)]
+    long_wire = [(H, (q,), ()) for q in range(n)]
+    long_wire += [((RX, RY, RZ)[k % 3], (3,), (0.1 * k - 1.0,)) for k in range(40)]
+    long_wire += [(CX, (3, 7), ()), (RY, (0,), (0.4,)), (RZ, (0,), (0.9,))]
+    mixed = (W.hea(n, 2, seed=1) + W.random_u3(n, 2, seed=2)
+             + [(CCX, (0, 4, 9), ()), (SWAP, (1, 8), ()), (CY, (10, 2), ()), (CZ, (3, 5), ()),
+                (T, (6,), ()), (S, (7,), ())] + W.qaoa_ring_seeded(n, 2, seed=3)[n:])
+    return {"qaoa_ring": W.qaoa_ring_seeded(n, 3, seed=8), "tfim": W.tfim_chain(n, 4),
+            "hea_d4": W.hea(n, 4, seed=5), "zz_many": zz_many, "long_wire": long_wire,
+            "mixed": mixed}
+
+
+@pytest.mark.parametrize("name", list(_fused_cases()))
+def test_fused_adjoint_matches_oracle_and_gate_by_gate(name):
+    n = 11
+    gates = _fused_cases()[name]
+    zterms = [(-1.0, 0, 0, (1 << q) | (1 << ((q + 1) % n))) for q in range(n)]
+    zterms += [(0.3, 0, 0, 1 << q) for q in range(0, n, 3)] + [(0.7, 0, 0, 0)]
+    mixed_terms = W.ring_tfim_hamiltonian(n, 0.7) + [(0.25, 0, 1 << 4, 1 << 2)]
+    for terms in (zterms, mixed_terms):
+        e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+        c, h = W.to_circuit(n, gates), W.to_hamiltonian(terms)
+        sim = qm.Simulator(n)
+        e1, g1 = sim.energy_and_gradient(c, h)                 # block-wise sweep
+        e2, g2 = sim.energy_and_gradient(c, h, fused=False)    # gate by gate
+        assert abs(e1 - e0) <= 1e-5 and abs(e2 - e0) <= 1e-5
+        assert np.abs(np.array(g1) - g0).max() <= 1e-5, name
+        assert np.abs(np.array(g2) - g0).max() <= 1e-5, name
+        for k, (_, _, ps) in enumerate(gates):
+            if not ps:
+                assert g1[k] == 0.0
+
+
+@pytest.mark.parametrize("n", [14, 18])
+def test_fused_adjoint_tiles_and_lanes(n):
+    """Large enough for whole 13-bit tiles plus tile bits in the generators."""
+    gates, terms = W.hea_gradient_problem(n, depth=3, seed=n)
+    gates = W.qaoa_ring_seeded(n, 2, seed=n) + gates
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    e1, g1 = qm.Simulator(n).energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+    assert abs(e1 - e0) <= 1e-5
+    assert np.abs(np.array(g1) - g0).max() <= 1e-5
+    zt = [(-0.5, 0, 0, (1 << a) | (1 << b)) for a, b in W.random_3regular(n, np.random.default_rng(n))]
+    e0, g0 = oracle.energy_and_gradient(n, gates, zt)
+    e1, g1 = qm.Simulator(n).energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(zt))
+    assert abs(e1 - e0) <= 1e-5
+    assert np.abs(np.array(g1) - g0).max() <= 1e-5
+
+
 def test_gradient_matches_oracle_adjoint_wide():
     """All gate kinds in the backward sweep, every wire, n = 12."""
     n = 12
