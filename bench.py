@@ -255,6 +255,8 @@ def run_batch_workload(args, world, rank, dist):
                      W.to_hamiltonian(W.maxcut_hamiltonian(inst["edges"])), 4096, 7000 + k))
     params = sum(len(c) for c, _h, _s, _seed in reqs)
 
+    tuning = qm.batch_autotune(reqs) if args.lanes == 0 else None
+
     def serve(mode):
         torch_sync()
         t0 = time.perf_counter()
@@ -306,7 +308,9 @@ def run_batch_workload(args, world, rank, dist):
             "data": "synthetic",
             "config": {"workload": f"{len(reqs)} QAOA MaxCut requests (energy + adjoint "
                                    "gradient + 4096 samples each)",
-                       "widths": widths, "gate_params": params, "lanes": args.lanes},
+                       "widths": widths, "gate_params": params,
+                       "lanes": tuning["lanes"] if tuning else args.lanes,
+                       "autotuned": tuning},
             "plain_loop": {"value": round(len(reqs) / plain_t, 2), "unit": "requests/s",
                            "seconds": round(plain_t, 3),
                            "what": "per-circuit loop: gate-by-gate adjoint, run, sample"},
@@ -394,7 +398,8 @@ def main():
     ap.add_argument("--workload", default="fused30", choices=["fused30", "batch", "grad"])
     ap.add_argument("--grad-qubits", type=int, nargs="+", default=[28, 33])
     ap.add_argument("--requests", type=int, default=512)
-    ap.add_argument("--lanes", type=int, default=8)
+    ap.add_argument("--lanes", type=int, default=0,
+                    help="batch lanes; 0 = autotuned on the batch's own requests")
     ap.add_argument("--cpu-qubits", type=int, default=N_CPU,
                     help="width of the bounded CPU sample (reference arm, cpu_baseline)")
     args = ap.parse_args()

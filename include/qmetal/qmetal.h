@@ -115,6 +115,15 @@ int qm_apply_gate(qm_simulator s, qm_gate_kind kind, const uint32_t *qubits,
                   uint32_t num_qubits, const double *params,
                   uint32_t num_params);
 
+/* qm_run through a CUDA graph: the first call for a circuit's content
+ * (width, gates, wires, parameter values) captures the default plan's
+ * launches on the simulator's stream; later calls with the same content
+ * replay that graph in one launch. Up to 16 graphs are kept per simulator,
+ * least recently used evicted. The reference has no counterpart (it encodes
+ * every run's dispatches into a fresh Metal command buffer,
+ * src/metal/simulator.mm:189-196 and 436-448). */
+int qm_run_cached(qm_simulator s, qm_circuit c);
+
 /* Run with explicit fusion options (FusionOptions, reference plan.h:76-94). */
 int qm_run_options(qm_simulator s, qm_circuit c, int collapse_1q_windows,
                    int fuse_diagonals, int recognize_zz, uint32_t group_1q,
@@ -169,8 +178,17 @@ typedef struct {
  * mode 1: one request after another as a per-circuit caller would run them
  *         (gate-by-gate adjoint, then run and sample);
  * mode 2: one request after another with the block-wise adjoint.
- * Every mode returns the same numbers to within float round-off. */
+ * Every mode returns the same numbers to within float round-off. In mode 0,
+ * lanes = 0 uses the autotuned lane count and tile shapes (tuning first if
+ * this set of widths has not been tuned in this process). */
 int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t lanes);
+
+/* Tune a batch on its own requests (their outputs are overwritten): per
+ * width, the number of wires >= 6 each backward window pass holds in
+ * registers (out_tile_high[n], qm_max_qubits() + 1 entries, may be NULL),
+ * then the lane count. Cached per set of widths for the process. */
+int qm_batch_autotune(const qm_batch_item *items, size_t count, uint32_t *out_lanes,
+                      uint32_t *out_tile_high, double *out_seconds);
 
 #ifdef __cplusplus
 }

@@ -36,9 +36,12 @@ int qmk_apply_1q(float *state, uint32_t n, uint32_t q, const float m[8],
 int qmk_apply_phase(float *state, uint32_t n, uint64_t mask, float re,
                     float im, void *stream);
 
-/* k in 2..5 commuting 2x2s on distinct ascending wires, one pass, amplitudes
- * held in registers. Replaces apply_1q_group{2,3,4} (kernels.metal:71-102;
- * simulator.mm:500-525). */
+/* k commuting 2x2s on distinct ascending wires in one pass: wire 0 pairs the
+ * lanes of each vector, wires 1..5 exchange with partner lanes by warp
+ * shuffle, wires >= 6 pair registers. One launch takes wire 0 plus up to five
+ * wires in 1..5 and four wires >= 6 (k <= 10), or, with no wire in 1..5,
+ * wire 0 plus up to five others. Replaces apply_1q_group{2,3,4}
+ * (kernels.metal:71-102; simulator.mm:500-525). */
 int qmk_apply_group(float *state, uint32_t n, uint32_t k,
                     const uint32_t *qubits, const float *matrices,
                     void *stream);

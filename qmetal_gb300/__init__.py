@@ -101,6 +101,7 @@ _destroy = _decl("qm_destroy", None, c_void_p)
 _reset = _decl("qm_reset", c_int, c_void_p)
 _run = _decl("qm_run", c_int, c_void_p, c_void_p)
 _run_unfused = _decl("qm_run_unfused", c_int, c_void_p, c_void_p)
+_run_cached = _decl("qm_run_cached", c_int, c_void_p, c_void_p)
 _run_options = _decl("qm_run_options", c_int, c_void_p, c_void_p, c_int, c_int,
                      c_int, c_uint32, c_uint32)
 _sync = _decl("qm_synchronize", c_int, c_void_p)
@@ -133,6 +134,8 @@ class _BatchItem(ctypes.Structure):
 
 
 _batch_serve = _decl("qm_batch_serve", c_int, POINTER(_BatchItem), c_size_t, c_int, c_uint32)
+_batch_autotune = _decl("qm_batch_autotune", c_int, POINTER(_BatchItem), c_size_t, _u32p, _u32p,
+                        _f64p)
 _run_profiled = _decl("qm_run_profiled", c_int, c_void_p, c_void_p, c_int, _f64p,
                       c_size_t, POINTER(c_size_t))
 
@@ -313,6 +316,12 @@ class Simulator:
         _check((_run if fuse else _run_unfused)(self._h, circuit._h))
         return self
 
+    def run_cached(self, circuit: Circuit):
+        """run() replayed from a CUDA graph captured on the first call with
+        this circuit's content (same kernels and results as run())."""
+        _check(_run_cached(self._h, circuit._h))
+        return self
+
     def run_options(self, circuit: Circuit, collapse=True, diagonals=True,
                     zz=True, group=4, block_bits=0):
         _check(_run_options(self._h, circuit._h, int(collapse), int(diagonals),
@@ -430,15 +439,11 @@ class Simulator:
 BATCH_LANES, BATCH_PLAIN_LOOP, BATCH_FUSED_LOOP = 0, 1, 2
 
 
-def batch_serve(requests, mode: int = BATCH_LANES, lanes: int = 8):
-    """Energy, adjoint gradient and samples for many (circuit, hamiltonian,
-    shots, seed) requests of any widths in one call. Returns a list of
-    (energy, gradient list, samples list), in request order."""
+def _batch_items(requests):
     import numpy as np
     reqs = list(requests)
     items = (_BatchItem * max(1, len(reqs)))()
-    keep = []
-    outs = []
+    keep, outs = [], []
     for i, (circ, ham, shots, seed) in enumerate(reqs):
         h = ham._c()
         e = np.zeros(1, dtype=np.float64)
@@ -453,5 +458,27 @@ def batch_serve(requests, mode: int = BATCH_LANES, lanes: int = 8):
         items[i].out_energy = e.ctypes.data_as(_f64p)
         items[i].out_grad = g.ctypes.data_as(_f64p)
         items[i].out_samples = s.ctypes.data_as(_u64p)
-    _check(_batch_serve(items, len(reqs), int(mode), int(lanes)))
+    return items, len(reqs), keep, outs
+
+
+def batch_serve(requests, mode: int = BATCH_LANES, lanes: int = 8):
+    """Energy, adjoint gradient and samples for many (circuit, hamiltonian,
+    shots, seed) requests of any widths in one call. Returns a list of
+    (energy, gradient list, samples list), in request order. lanes=0 uses
+    the autotuned lane count and tile shapes."""
+    items, count, _keep, outs = _batch_items(requests)
+    _check(_batch_serve(items, count, int(mode), int(lanes)))
     return [(float(e[0]), g[:ng].tolist(), s[:ns].tolist()) for e, g, s, ng, ns in outs]
+
+
+def batch_autotune(requests):
+    """Tune a batch on its own requests; returns {"lanes", "tile_high"
+    (width -> wires >= 6 per backward pass), "seconds"}."""
+    items, count, _keep, _outs = _batch_items(requests)
+    lanes = c_uint32()
+    tile = (c_uint32 * (max_qubits() + 1))()
+    secs = c_double()
+    _check(_batch_autotune(items, count, byref(lanes), tile, byref(secs)))
+    widths = sorted({int(c.num_qubits) for c, _h, _s, _seed in requests})
+    return {"lanes": int(lanes.value), "seconds": float(secs.value),
+            "tile_high": {n: int(tile[n]) for n in widths if n >= 7}}

@@ -25,6 +25,24 @@ enum class BatchMode {
   FusedLoop = 2,   // one request after another, block-wise adjoint
 };
 
+// Choices the autotuner makes for a batch: how many lanes run at once, and per
+// width the tile shape of the backward window passes (wires >= 6 held in
+// registers per pass).
+struct BatchTuning {
+  uint32_t lanes = 8;
+  uint32_t tile_high[kMaxQubits + 1];
+  double seconds = 0.0;   // time spent measuring
+  BatchTuning() {
+    for (auto &t : tile_high) t = 4;
+  }
+};
+
+// Measure candidates on the batch's own requests: per width, one request
+// served with each tile shape; then a quarter of the batch served with each
+// lane count. Results are cached per set of widths for the process.
+BatchTuning autotune_batch(const std::vector<BatchItem> &items);
+
+// lanes == 0 in Lanes mode: use (and if needed compute) the autotuned choices.
 void run_batch(const std::vector<BatchItem> &items, BatchMode mode, uint32_t lanes);
 
 }  // namespace qmetal

@@ -215,6 +215,14 @@ int qm_run(qm_simulator s, qm_circuit c) {
   return guarded([&] { s->s->run(c->c); });
 }
 
+int qm_run_cached(qm_simulator s, qm_circuit c) {
+  if (!s || !c) {
+    set_error("null argument");
+    return -1;
+  }
+  return guarded([&] { s->s->run_cached(c->c); });
+}
+
 int qm_run_unfused(qm_simulator s, qm_circuit c) {
   if (!s || !c) {
     set_error("null argument");
@@ -425,6 +433,34 @@ int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t 
       v[i].samples = items[i].out_samples;
     }
     run_batch(v, static_cast<BatchMode>(mode), lanes);
+  });
+}
+
+int qm_batch_autotune(const qm_batch_item *items, size_t count, uint32_t *out_lanes,
+                      uint32_t *out_tile_high, double *out_seconds) {
+  if (!count || !items) {
+    set_error("null argument");
+    return -1;
+  }
+  return guarded([&] {
+    std::vector<Hamiltonian> hams(count);
+    std::vector<BatchItem> v(count);
+    for (size_t i = 0; i < count; i++) {
+      if (!items[i].circuit || !items[i].hamiltonian)
+        throw std::runtime_error("batch: null circuit or Hamiltonian");
+      hams[i] = hamiltonian_of(items[i].hamiltonian);
+      v[i].circuit = &items[i].circuit->c;
+      v[i].hamiltonian = &hams[i];
+      v[i].shots = items[i].shots;
+      v[i].seed = items[i].seed;
+      v[i].energy = items[i].out_energy;
+      v[i].grad = items[i].out_grad;
+      v[i].samples = items[i].out_samples;
+    }
+    const BatchTuning t = autotune_batch(v);
+    if (out_lanes) *out_lanes = t.lanes;
+    if (out_tile_high) std::copy(t.tile_high, t.tile_high + kMaxQubits + 1, out_tile_high);
+    if (out_seconds) *out_seconds = t.seconds;
   });
 }
 

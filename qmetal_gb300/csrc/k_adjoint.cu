@@ -288,6 +288,160 @@ k_adj_group(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsites,
   if constexpr (NG > 0) finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
 }
 
+// ---------------------------------------------------------------------------
+// Wider window tiles for both states: a warp owns 32 consecutive vectors
+// (lane = vector bits 0..4, i.e. wires 1..5) for every combination of up to
+// KH wires >= 6 held in registers, so all accesses are full 512-byte warp
+// accesses. Wire 0 pairs the lanes of a vector; a wire in 1..5 exchanges
+// with the partner lane by shuffle, and each lane then takes its own half of
+// the overlap (the two halves of a pair sum to the pair's term).
+
+constexpr int kMaxWarpOps = 32;
+
+struct WarpAdjArgs {
+  uint32_t nops, ngrad;
+  uint32_t hpos[4];              // wires >= 6: vector bit - 5, ascending
+  int8_t kind[kMaxWarpOps];      // 0: wire 0, 1: lane bit, 2: register bit
+  int8_t arg[kMaxWarpOps];       // lane bit (0..4) or register index
+  int8_t gen[kMaxWarpOps];
+  int8_t slotidx[kMaxWarpOps];
+  M2 m[kMaxWarpOps];
+};
+
+// Im(conj(l_own) (P psi)_own) for one element of a pair; one = the element's
+// wire bit.
+__device__ __forceinline__ float own_term(int gen, float2 p0, float2 p1, float2 l0, float2 l1,
+                                          bool one) {
+  float2 w, l;
+  if (gen == 1) {
+    w = one ? p0 : p1;
+  } else if (gen == 2) {
+    w = one ? make_float2(-p0.y, p0.x) : make_float2(p1.y, -p1.x);
+  } else {
+    w = one ? make_float2(-p1.x, -p1.y) : p0;
+  }
+  l = one ? l1 : l0;
+  return l.x * w.y - l.y * w.x;
+}
+
+__device__ __forceinline__ float4 shfl4(const float4 &v, int mask) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask),
+                     __shfl_xor_sync(0xffffffffu, v.z, mask), __shfl_xor_sync(0xffffffffu, v.w, mask));
+}
+
+template <int KH, int NG>
+__global__ void __launch_bounds__(kThreads)
+k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, WarpAdjArgs g,
+           Area a, OutSlots<(NG > 0 ? NG : 1)> out) {
+  constexpr int NV = 1 << KH;
+  constexpr int NA = NG > 0 ? NG : 1;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
+  double acc[NA];
+#pragma unroll
+  for (int t = 0; t < NA; t++) acc[t] = 0.0;
+  for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
+    uint64_t b = ws;
+#pragma unroll
+    for (int j = 0; j < KH; j++) b = ins0(b, g.hpos[j]);
+    const uint64_t base = (b << 5) | lane;
+    float4 P[NV], L[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      P[l] = psi[v];
+      L[l] = lam[v];
+    }
+    float part[NA];
+#pragma unroll
+    for (int t = 0; t < NA; t++) part[t] = 0.0f;
+    for (uint32_t o = 0; o < g.nops; o++) {
+      const int kind = g.kind[o], arg = g.arg[o], gen = g.gen[o];
+      const M2 m = g.m[o];
+      float ov = 0.0f;
+      if (kind == 0) {
+#pragma unroll
+        for (int l = 0; l < NV; l++) {
+          float2 p0 = lo2(P[l]), p1 = hi2(P[l]), l0 = lo2(L[l]), l1 = hi2(L[l]);
+          if (gen) ov += overlap(gen, p0, p1, l0, l1);
+          apply2(m, p0, p1);
+          apply2(m, l0, l1);
+          P[l] = pack4(p0, p1);
+          L[l] = pack4(l0, l1);
+        }
+      } else if (kind == 1) {
+        const bool one = (lane >> arg) & 1;
+        const float2 c0 = one ? m.c : m.a, c1 = one ? m.d : m.b;
+#pragma unroll
+        for (int l = 0; l < NV; l++) {
+          const float4 Po = shfl4(P[l], 1 << arg), Lo = shfl4(L[l], 1 << arg);
+          const float4 p0 = one ? Po : P[l], p1 = one ? P[l] : Po;
+          const float4 l0 = one ? Lo : L[l], l1 = one ? L[l] : Lo;
+          if (gen)
+            ov += own_term(gen, lo2(p0), lo2(p1), lo2(l0), lo2(l1), one) +
+                  own_term(gen, hi2(p0), hi2(p1), hi2(l0), hi2(l1), one);
+          P[l] = pack4(cmac2(c0, lo2(p0), c1, lo2(p1)), cmac2(c0, hi2(p0), c1, hi2(p1)));
+          L[l] = pack4(cmac2(c0, lo2(l0), c1, lo2(l1)), cmac2(c0, hi2(l0), c1, hi2(l1)));
+        }
+      } else {
+#pragma unroll
+        for (int j = 0; j < KH; j++) {
+          if (j != arg) continue;
+#pragma unroll
+          for (int l = 0; l < NV; l++) {
+            if ((l >> j) & 1) continue;
+            const int h = l | (1 << j);
+            float2 pa = lo2(P[l]), pb = lo2(P[h]), qa = hi2(P[l]), qb = hi2(P[h]);
+            float2 la = lo2(L[l]), lb = lo2(L[h]), ma = hi2(L[l]), mb = hi2(L[h]);
+            if (gen) ov += overlap(gen, pa, pb, la, lb) + overlap(gen, qa, qb, ma, mb);
+            apply2(m, pa, pb);
+            apply2(m, qa, qb);
+            apply2(m, la, lb);
+            apply2(m, ma, mb);
+            P[l] = pack4(pa, qa);
+            P[h] = pack4(pb, qb);
+            L[l] = pack4(la, ma);
+            L[h] = pack4(lb, mb);
+          }
+        }
+      }
+      if (NG > 0 && gen) {
+#pragma unroll
+        for (int t = 0; t < NA; t++)
+          if (t == g.slotidx[o]) part[t] += ov;
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      psi[v] = P[l];
+      lam[v] = L[l];
+    }
+#pragma unroll
+    for (int t = 0; t < NA; t++) acc[t] += part[t];
+  }
+  if constexpr (NG > 0) finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
+}
+
+template <int KH, int NG>
+void launch_adj_warp(float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArgs &g,
+                     const OutSlots<kMaxGen> &slots, Area a, cudaStream_t s) {
+  OutSlots<(NG > 0 ? NG : 1)> out{};
+  out.p = slots.p;
+  for (int t = 0; t < (NG > 0 ? NG : 1); t++) out.slot[t] = slots.slot[t];
+  const uint64_t per_block = kThreads / 32;
+  unsigned grid = grid_for(nwsites, per_block);
+  if (NG > 0) grid = std::min<unsigned>(grid, reduce_grid());
+  k_adj_warp<KH, NG><<<grid, kThreads, 0, s>>>(psi, lam, nwsites, g, a, out);
+}
+
 bool ok_ws(void *ws, size_t bytes, uint32_t n) {
   return ws && bytes >= qmk_workspace_bytes(n);
 }
@@ -418,12 +572,12 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
                                  const uint32_t *wires, const float *minv, const int *gens,
                                  const uint32_t *slots, double *d_grad, void *ws, size_t ws_bytes,
                                  void *stream) {
-  if (!psi || !lam || n < 1 || n > 40 || nops < 1 || nops > kMaxOps || !wires || !minv || !gens ||
-      !ok_ws(ws, ws_bytes, n))
+  if (!psi || !lam || n < 1 || n > 40 || nops < 1 || nops > kMaxWarpOps || !wires || !minv ||
+      !gens || !ok_ws(ws, ws_bytes, n))
     return -1;
   // Distinct wires of the tile.
-  uint32_t distinct[kMaxOps];
-  uint32_t nd = 0;
+  uint32_t distinct[kMaxWarpOps], high[kMaxWarpOps];
+  uint32_t nd = 0, nh = 0;
   bool w0 = false;
   int ngrad = 0;
   for (uint32_t o = 0; o < nops; o++) {
@@ -436,9 +590,64 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
     }
     bool seen = false;
     for (uint32_t k = 0; k < nd; k++) seen |= distinct[k] == wires[o];
-    if (!seen) distinct[nd++] = wires[o];
+    if (!seen) {
+      distinct[nd++] = wires[o];
+      if (wires[o] >= 6) high[nh++] = wires[o];
+    }
   }
-  if (nd > 3 || n - 1 < nd) return -1;
+  if (ngrad > 16) return -1;
+  if (nh <= 4 && n >= 6 + nh) {
+    // Warp tile: lanes carry wires 1..5, registers the wires >= 6.
+    std::sort(high, high + nh);
+    WarpAdjArgs g{};
+    OutSlots<kMaxGen> out{};
+    out.p = d_grad;
+    g.nops = nops;
+    g.ngrad = static_cast<uint32_t>(ngrad);
+    for (uint32_t k = 0; k < nh; k++) g.hpos[k] = high[k] - 6;
+    int gi = 0;
+    for (uint32_t o = 0; o < nops; o++) {
+      const uint32_t q = wires[o];
+      if (q == 0) {
+        g.kind[o] = 0;
+        g.arg[o] = 0;
+      } else if (q <= 5) {
+        g.kind[o] = 1;
+        g.arg[o] = static_cast<int8_t>(q - 1);
+      } else {
+        g.kind[o] = 2;
+        g.arg[o] = static_cast<int8_t>(std::find(high, high + nh, q) - high);
+      }
+      g.gen[o] = static_cast<int8_t>(gens[o]);
+      g.m[o] = m2_from(minv + 8 * o);
+      g.slotidx[o] = -1;
+      if (gens[o]) {
+        g.slotidx[o] = static_cast<int8_t>(gi);
+        out.slot[gi] = slots[o];
+        gi++;
+      }
+    }
+    const uint64_t nw = 1ull << (n - 6 - nh);
+    float4 *p4 = reinterpret_cast<float4 *>(psi), *l4 = reinterpret_cast<float4 *>(lam);
+    cudaStream_t s = (cudaStream_t)stream;
+    const Area a = area_of(ws);
+    const int ng = ngrad == 0 ? 0 : (ngrad <= 4 ? 4 : (ngrad <= 8 ? 8 : 16));
+#define QMK_ADJ_WARP_CASE(KH)                                                   \
+    if (nh == KH) {                                                             \
+      if (ng == 0) launch_adj_warp<KH, 0>(p4, l4, nw, g, out, a, s);            \
+      else if (ng == 4) launch_adj_warp<KH, 4>(p4, l4, nw, g, out, a, s);       \
+      else if (ng == 8) launch_adj_warp<KH, 8>(p4, l4, nw, g, out, a, s);       \
+      else launch_adj_warp<KH, 16>(p4, l4, nw, g, out, a, s);                   \
+    }
+    QMK_ADJ_WARP_CASE(0)
+    QMK_ADJ_WARP_CASE(1)
+    QMK_ADJ_WARP_CASE(2)
+    QMK_ADJ_WARP_CASE(3)
+    QMK_ADJ_WARP_CASE(4)
+#undef QMK_ADJ_WARP_CASE
+    return launch_status();
+  }
+  if (nd > 3 || n - 1 < nd || nops > kMaxOps) return -1;
   std::sort(distinct, distinct + nd);
   GroupAdjArgs g{};
   OutSlots<kMaxOps> out{};

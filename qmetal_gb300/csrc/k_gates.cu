@@ -455,7 +455,7 @@ static void launch_group(float4 *st, uint64_t nsites, const GroupArgs &g,
 extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
                                const uint32_t *qubits, const float *mats,
                                void *stream) {
-  if (!valid_state(state, n) || k < 1 || k > 5 || !qubits || !mats) return -1;
+  if (!valid_state(state, n) || k < 1 || k > 10 || !qubits || !mats) return -1;
   for (uint32_t j = 0; j < k; j++) {
     if (qubits[j] >= n) return -1;
     if (j && qubits[j] <= qubits[j - 1]) return -1;  // ascending, distinct
@@ -496,11 +496,14 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
         case 5: k_group_warp<2, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
         case 6: k_group_warp<3, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
         case 7: k_group_warp<3, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        default: k_group_warp<4, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 8: k_group_warp<4, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 9: k_group_warp<4, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        default: return -1;
       }
       return launch_status();
     }
   }
+  if (k - (w0 ? 1u : 0u) > 5) return -1;  // register path: at most five wires >= 1
   GroupArgs g{};
   int kp = 0;
   for (uint32_t j = 0; j < k; j++) {
@@ -525,6 +528,7 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
     case 8: launch_group<4, false>(st, nsites, g, s); break;
     case 9: launch_group<4, true>(st, nsites, g, s); break;
     case 10: launch_group<5, false>(st, nsites, g, s); break;
+    case 11: launch_group<5, true>(st, nsites, g, s); break;
     default: return -1;
   }
   return launch_status();

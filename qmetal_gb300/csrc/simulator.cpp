@@ -174,6 +174,8 @@ Simulator::~Simulator() { release(); }
 
 void Simulator::release() {
   if (stream_) cudaStreamSynchronize(S(stream_));
+  for (const GraphEntry &e : graphs_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(e.exec));
+  graphs_.clear();
   cudaFree(state_);
   cudaFree(costate_);
   cudaFree(ws_);
@@ -301,6 +303,149 @@ void Simulator::run(const Plan &p) {
 void Simulator::apply(const PlanOp &op) {
   activate();
   apply_op_to(state_, op);
+}
+
+namespace {
+
+// FNV-1a over the circuit's content (width, kinds, wires, parameter bits).
+uint64_t circuit_key(const Circuit &c) {
+  uint64_t h = 1469598103934665603ull;
+  auto mix = [&](const void *p, size_t n) {
+    const unsigned char *b = static_cast<const unsigned char *>(p);
+    for (size_t i = 0; i < n; i++) {
+      h ^= b[i];
+      h *= 1099511628211ull;
+    }
+  };
+  mix(&c.num_qubits, sizeof(c.num_qubits));
+  const uint64_t count = c.ops.size();
+  mix(&count, sizeof(count));
+  for (const Gate &g : c.ops) {
+    mix(&g.kind, 1);
+    mix(&g.num_qubits, 1);
+    mix(&g.num_params, 1);
+    mix(g.qubits, sizeof(uint32_t) * g.num_qubits);
+    mix(g.params, sizeof(double) * g.num_params);
+  }
+  return h;
+}
+
+constexpr size_t kMaxGraphs = 16;
+
+}  // namespace
+
+void Simulator::run_cached(const Circuit &c) {
+  if (c.num_qubits != n_) throw std::runtime_error("circuit/simulator size mismatch");
+  activate();
+  const uint64_t key = circuit_key(c);
+  for (size_t i = 0; i < graphs_.size(); i++) {
+    if (graphs_[i].key != key) continue;
+    GraphEntry e = graphs_[i];
+    graphs_.erase(graphs_.begin() + i);
+    graphs_.push_back(e);
+    cuda_check(cudaGraphLaunch(static_cast<cudaGraphExec_t>(e.exec), S(stream_)), "graph launch");
+    dispatches_ += e.launches;
+    return;
+  }
+  const Plan plan = build_plan(c, FusionOptions{});
+  const uint64_t before = dispatches_;
+  cuda_check(cudaStreamBeginCapture(S(stream_), cudaStreamCaptureModeThreadLocal), "graph capture");
+  cudaGraph_t graph = nullptr;
+  try {
+    for (const PlanOp &op : plan.ops) apply_op_to(state_, op);
+  } catch (...) {
+    cudaStreamEndCapture(S(stream_), &graph);
+    if (graph) cudaGraphDestroy(graph);
+    dispatches_ = before;
+    throw;
+  }
+  cuda_check(cudaStreamEndCapture(S(stream_), &graph), "graph capture");
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  cuda_check(e, "graph instantiate");
+  const uint64_t launches = dispatches_ - before;
+  if (graphs_.size() == kMaxGraphs) {
+    cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(graphs_.front().exec));
+    graphs_.erase(graphs_.begin());
+  }
+  graphs_.push_back({key, exec, launches});
+  cuda_check(cudaGraphLaunch(exec, S(stream_)), "graph launch");
+}
+
+// The plan with consecutive one-qubit ops merged into wider group passes.
+// The plan emits a window's 2x2 products as Dense1q / Dense1qGroup ops on
+// distinct wires, which commute, so any set of them can share one pass: wire
+// 0, up to five of wires 1..5 (warp shuffles) and four wires >= 6
+// (registers), or wire 0 and five wires >= 1 in registers.
+void Simulator::run_merged(const Plan &p) {
+  if (p.num_qubits != n_) throw std::runtime_error("plan/simulator size mismatch");
+  activate();
+  std::vector<uint32_t> wires;
+  std::vector<cdouble> mats;
+  auto fits = [&](const std::vector<uint32_t> &w) {
+    uint32_t lane = 0, high = 0, zero = 0;
+    for (uint32_t q : w) {
+      if (q == 0) zero++;
+      else if (q <= 5) lane++;
+      else high++;
+    }
+    if (zero > 1) return false;
+    if (lane >= 1 && lane <= 5 && high <= 4 && n_ >= 6 + high) return true;
+    return lane + high <= 5;
+  };
+  auto flush = [&]() {
+    if (wires.empty()) return;
+    std::vector<size_t> order(wires.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return wires[a] < wires[b]; });
+    std::vector<uint32_t> ws;
+    std::vector<float> fm(8 * wires.size());
+    for (size_t i = 0; i < order.size(); i++) {
+      ws.push_back(wires[order[i]]);
+      narrow(&mats[4 * order[i]], &fm[8 * i]);
+    }
+    check(qmk_apply_group(state_, n_, static_cast<uint32_t>(ws.size()), ws.data(), fm.data(),
+                          stream_),
+          "merged group");
+    dispatches_++;
+    wires.clear();
+    mats.clear();
+  };
+  for (const PlanOp &op : p.ops) {
+    std::vector<uint32_t> w;
+    std::vector<cdouble> m;
+    if (op.kind == PlanOp::Kind::Dense1q) {
+      w.push_back(op.qubits[0]);
+      m.assign(op.matrix, op.matrix + 4);
+    } else if (op.kind == PlanOp::Kind::Dense1qGroup) {
+      w = op.group_qubits;
+      m = op.group_matrices;
+    } else {
+      flush();
+      apply_op_to(state_, op);
+      continue;
+    }
+    for (uint32_t q : w)
+      if (q >= n_) throw std::runtime_error("qubit index out of range");
+    std::vector<uint32_t> all = wires;
+    bool overlap = false;
+    for (uint32_t q : w) {
+      if (std::find(wires.begin(), wires.end(), q) != wires.end()) overlap = true;
+      all.push_back(q);
+    }
+    if (overlap || !fits(all)) flush();
+    // A group wider than one pass (never emitted by the default passes) goes
+    // wire by wire.
+    for (size_t j = 0; j < w.size(); j++) {
+      std::vector<uint32_t> trial = wires;
+      trial.push_back(w[j]);
+      if (!fits(trial)) flush();
+      wires.push_back(w[j]);
+      mats.insert(mats.end(), m.begin() + 4 * j, m.begin() + 4 * j + 4);
+    }
+  }
+  flush();
 }
 
 void Simulator::run_profiled(const Plan &p, std::vector<double> &seconds) {
@@ -819,8 +964,11 @@ void Simulator::sweep_fused(const Circuit &c) {
     std::vector<std::vector<size_t>> per_wire(n_);
     for (size_t k = seg.begin; k < seg.end; k++) per_wire[c.ops[k].qubits[0]].push_back(k);
     std::vector<WireOp> tile;
-    uint32_t others = 0, grads = 0;
+    uint32_t others = 0, highs = 0, grads = 0;
     bool tile_has_param = false;
+    const bool wide = n_ >= 6;
+    const uint32_t max_ops = wide ? 32u : kOps;
+    const uint32_t max_high = wide ? std::min<uint32_t>(tile_high_, n_ - 6) : 0;
     auto flush = [&]() {
       if (tile.empty()) return;
       if (undo || tile_has_param) {
@@ -840,7 +988,7 @@ void Simulator::sweep_fused(const Circuit &c) {
         dispatches_++;
       }
       tile.clear();
-      others = grads = 0;
+      others = highs = grads = 0;
       tile_has_param = false;
     };
     for (uint32_t w = 0; w < n_; w++) {
@@ -861,8 +1009,8 @@ void Simulator::sweep_fused(const Circuit &c) {
         if (o.gen) wgrads++;
         ops.push_back(o);
       }
-      const uint32_t need_other = w != 0 ? 1u : 0u;
-      if (ops.size() > kOps) {
+      const uint32_t need_other = w != 0 ? 1u : 0u, need_high = w >= 6 ? 1u : 0u;
+      if (ops.size() > max_ops || wgrads > 16) {
         flush();
         for (size_t b = 0; b < ops.size(); b += kOps) {
           const size_t e = std::min(ops.size(), b + kOps);
@@ -872,11 +1020,19 @@ void Simulator::sweep_fused(const Circuit &c) {
         }
         continue;
       }
-      const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;
-      if (tile.size() + ops.size() > kOps || others + need_other > 3 || grads + wgrads > cap)
-        flush();
+      bool full;
+      if (wide) {
+        // Warp tiles: wire 0, wires 1..5 in the lanes, up to four wires >= 6.
+        full = tile.size() + ops.size() > max_ops || highs + need_high > max_high ||
+               grads + wgrads > 16;
+      } else {
+        const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;
+        full = tile.size() + ops.size() > kOps || others + need_other > 3 || grads + wgrads > cap;
+      }
+      if (full) flush();
       tile.insert(tile.end(), ops.begin(), ops.end());
       others += need_other;
+      highs += need_high;
       grads += wgrads;
       tile_has_param |= wgrads > 0;
     }
@@ -891,10 +1047,13 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
   const size_t G = c.ops.size();
   std::vector<double> grad(G, 0.0);
   try {
-    // Forward: the fused plan reaches the same final state as the gate
-    // stream; only the backward sweep needs per-gate identity.
+    // Forward: the fused plan (merged passes) reaches the same final state as
+    // the gate stream; only the backward sweep needs per-gate identity. The
+    // reference's algorithm (fused = false) runs the forward gate by gate, as
+    // src/metal/simulator.mm:840-845 does.
     reset();
-    run(build_plan(c, FusionOptions{}));
+    if (fused) run_merged(build_plan(c, FusionOptions{}));
+    else run(build_plan(c, FusionOptions::none()));
     energy_and_costate(h);
     if (fused) sweep_fused(c);
     else sweep_gate_by_gate(c);
@@ -917,7 +1076,7 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
   prepare_adjoint(c, h);
   try {
     reset();
-    run(build_plan(c, FusionOptions{}));
+    run_merged(build_plan(c, FusionOptions{}));
     if (shots) launch_sample(shots, seed);
     energy_and_costate(h);
     sweep_fused(c);

@@ -31,6 +31,13 @@ class Simulator {
   void run(const Circuit &c, const FusionOptions &opts);
   void run(const Plan &p);
   void apply(const PlanOp &op);
+  // run(c) through a CUDA graph: the first call for a given circuit content
+  // captures the plan's launches on this simulator's stream, later calls
+  // replay the graph with one launch. Same kernels, same results.
+  void run_cached(const Circuit &c);
+  // The plan with each window's consecutive one-qubit ops merged into as few
+  // group passes as the tile allows (same unitary, fewer passes).
+  void run_merged(const Plan &p);
   // Runs the plan with a CUDA event between ops; seconds[i] = op i's device time.
   void run_profiled(const Plan &p, std::vector<double> &seconds);
   void synchronize();
@@ -61,6 +68,12 @@ class Simulator {
   // one queued sequence with a single synchronisation.
   void serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint64_t seed, double *energy,
              double *grad, uint64_t *samples);
+
+  // Tile shape of the block-wise sweep's window passes: how many wires >= 6
+  // one two-state pass holds in registers (1..4, besides wire 0 and the five
+  // lane wires). Chosen per width by the batch autotuner.
+  void set_tile_high(uint32_t k) { tile_high_ = k < 1 ? 1 : (k > 4 ? 4 : k); }
+  uint32_t tile_high() const { return tile_high_; }
 
   uint64_t dispatch_count() const { return dispatches_; }
   double elapsed();
@@ -104,6 +117,13 @@ class Simulator {
   bool mirror_pinned_ = false;
   void *ev_start_ = nullptr, *ev_stop_ = nullptr;
   uint64_t dispatches_ = 0;
+  uint32_t tile_high_ = 4;
+  struct GraphEntry {
+    uint64_t key;
+    void *exec;         // cudaGraphExec_t
+    uint64_t launches;  // kernels in the graph
+  };
+  std::vector<GraphEntry> graphs_;   // most recent last
   bool fault_launch_ = false;
 };
 

@@ -1,0 +1,109 @@
+"""qmk_apply_group through the C ABI, on every route it takes.
+
+One launch applies k commuting 2x2s on distinct wires: wire 0 within a
+vector, wires 1..5 by warp shuffle, up to four wires >= 6 in registers
+(k <= 10), or wire 0 plus up to five others in registers. Each case draws a
+wire set for one route and compares the state with the same matrices applied
+one wire at a time in complex128 (tolerance 1e-5, as the other amplitude
+tests). Wire sets outside every route must be rejected without a launch.
+"""
+import ctypes
+from ctypes import c_int, c_uint32, c_void_p
+
+import numpy as np
+import pytest
+
+import qmetal_gb300 as qm
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-5
+
+
+def _lib():
+    L = ctypes.CDLL(qm.library_path())
+    L.qmk_apply_group.restype = c_int
+    L.qmk_apply_group.argtypes = [c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p]
+    return L
+
+
+def _unitary(rng):
+    z = rng.normal(size=(2, 2)) + 1j * rng.normal(size=(2, 2))
+    q, r = np.linalg.qr(z)
+    return q * (np.diag(r) / np.abs(np.diag(r)))
+
+
+def _apply_ref(state, n, wires, mats):
+    psi = state.reshape([2] * n)            # axis n-1-q is wire q (LSB first)
+    for q, m in zip(wires, mats):
+        ax = n - 1 - q
+        psi = np.moveaxis(np.tensordot(m, psi, axes=([1], [ax])), 0, ax)
+    return psi.reshape(-1)
+
+
+def _route_cases(n, rng):
+    """(wires) for each route the launch can take at width n."""
+    cases = []
+    for w0 in (False, True):
+        for nlow in range(0, 6):
+            for nhigh in range(0, min(4, n - 6) + 1):
+                if nlow == 0 and not w0 and nhigh == 0:
+                    continue
+                low = sorted(rng.choice(np.arange(1, 6), size=nlow, replace=False).tolist())
+                high = sorted(rng.choice(np.arange(6, n), size=nhigh, replace=False).tolist()) \
+                    if nhigh else []
+                cases.append(([0] if w0 else []) + low + high)
+    # register route: wire 0 and up to five wires >= 1, none in 1..5
+    if n >= 8:
+        for k in range(1, min(5, n - 6) + 1):
+            high = sorted(rng.choice(np.arange(6, n), size=k, replace=False).tolist())
+            cases.append([0] + high)
+    return cases
+
+
+@pytest.mark.parametrize("n", [6, 7, 9, 10, 11, 14])
+def test_every_route_matches_complex128(n):
+    torch = pytest.importorskip("torch")
+    L = _lib()
+    rng = np.random.default_rng(100 + n)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    host = np.empty(2 << n, dtype=np.float32)
+    host[0::2] = init.real
+    host[1::2] = init.imag
+    for wires in _route_cases(n, rng):
+        mats = [_unitary(rng) for _ in wires]
+        flat = np.empty(8 * len(wires), dtype=np.float32)
+        for j, m in enumerate(mats):
+            flat[8 * j:8 * j + 8] = [m[0, 0].real, m[0, 0].imag, m[0, 1].real, m[0, 1].imag,
+                                     m[1, 0].real, m[1, 0].imag, m[1, 1].real, m[1, 1].imag]
+        qs = np.array(wires, dtype=np.uint32)
+        dev = torch.from_numpy(host.copy()).cuda()
+        rc = L.qmk_apply_group(dev.data_ptr(), n, len(wires), qs.ctypes.data,
+                               flat.ctypes.data, None)
+        assert rc == 0, (n, wires)
+        torch.cuda.synchronize()
+        out = dev.cpu().numpy()
+        got = out[0::2].astype(np.float64) + 1j * out[1::2]
+        want = _apply_ref(init.copy(), n, wires, mats)
+        assert np.abs(got - want).max() <= TOL, (n, wires)
+
+
+def test_rejects_wire_sets_outside_every_route():
+    torch = pytest.importorskip("torch")
+    L = _lib()
+    n = 12
+    dev = torch.zeros(2 << n, dtype=torch.float32, device="cuda")
+    flat = np.tile(np.array([1, 0, 0, 0, 0, 0, 1, 0], dtype=np.float32), 11)
+    bad = [
+        [1, 6, 7, 8, 9, 10],          # five wires >= 6 beside a lane wire
+        [0, 6, 7, 8, 9, 10, 11],      # six register wires beside wire 0
+        [3, 2],                       # not ascending
+        [4, 4],                       # repeated
+        [0, 12],                      # out of range
+    ]
+    for wires in bad:
+        qs = np.array(wires, dtype=np.uint32)
+        assert L.qmk_apply_group(dev.data_ptr(), n, len(wires), qs.ctypes.data,
+                                 flat.ctypes.data, None) != 0, wires
+    qs = np.arange(11, dtype=np.uint32)
+    assert L.qmk_apply_group(dev.data_ptr(), n, 11, qs.ctypes.data, flat.ctypes.data, None) != 0
