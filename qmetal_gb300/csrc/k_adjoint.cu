@@ -110,9 +110,10 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
   __shared__ float2 Y2[1 << (kWMax - 6)];
   __shared__ float Fs[T > 0 ? kThreads * 33 : 1];
   const uint32_t W = d->W, tid = threadIdx.x, nv = 1u << (W - 1);
-  double acc[T > 0 ? T : 1];
+  // FP32 per thread over its tiles (a few dozen at most), FP64 from the warp up.
+  float accf[T > 0 ? T : 1];
 #pragma unroll
-  for (int t = 0; t < (T > 0 ? T : 1); t++) acc[t] = 0.0;
+  for (int t = 0; t < (T > 0 ? T : 1); t++) accf[t] = 0.0f;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
     if (g.undo) {
       tile_coeffs<true>(d, tile, f, &eH, nullptr, nullptr, true);
@@ -124,26 +125,43 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
     float F[32];
 #pragma unroll
     for (int j = 0; j < 32; j++) F[j] = 0.0f;
+    // Four vectors of both states (and their table entries) are loaded
+    // before any is used, so each thread keeps 8-12 loads in flight.
+    constexpr int UU = 4;
 #pragma unroll
-    for (int k = 0; k < 16; k++) {
-      const uint32_t e = tid + k * kThreads;
-      if (e >= nv) continue;
-      float4 p = psi[base + e], l = lam[base + e];
-      if (T > 0) {
-        F[2 * k] = l.x * p.y - l.y * p.x;
-        F[2 * k + 1] = l.z * p.w - l.w * p.z;
+    for (int c = 0; c < 16; c += UU) {
+      float4 P[UU], L[UU], tb[UU];
+#pragma unroll
+      for (int u = 0; u < UU; u++) {
+        const uint32_t e = tid + (c + u) * kThreads;
+        if (e < nv) {
+          P[u] = psi[base + e];
+          L[u] = lam[base + e];
+          if (g.undo) tb[u] = table4[e];
+        }
       }
-      if (g.undo) {
-        const uint32_t lo = 2 * e;
-        const float4 t = table4[e];
-        const float4 y1 = *reinterpret_cast<const float4 *>(&Y1[lo & 63]);
-        const float2 y2 = Y2[lo >> 6];
-        const float2 f0 = cmul(cmul(make_float2(t.x, -t.y), lo2(y1)), y2);
-        const float2 f1 = cmul(cmul(make_float2(t.z, -t.w), hi2(y1)), y2);
-        p = pack4(cmul(f0, lo2(p)), cmul(f1, hi2(p)));
-        l = pack4(cmul(f0, lo2(l)), cmul(f1, hi2(l)));
-        psi[base + e] = p;
-        lam[base + e] = l;
+#pragma unroll
+      for (int u = 0; u < UU; u++) {
+        const int k = c + u;
+        const uint32_t e = tid + k * kThreads;
+        if (e >= nv) continue;
+        float4 p = P[u], l = L[u];
+        if (T > 0) {
+          F[2 * k] = l.x * p.y - l.y * p.x;
+          F[2 * k + 1] = l.z * p.w - l.w * p.z;
+        }
+        if (g.undo) {
+          const uint32_t lo = 2 * e;
+          const float4 t = tb[u];
+          const float4 y1 = *reinterpret_cast<const float4 *>(&Y1[lo & 63]);
+          const float2 y2 = Y2[lo >> 6];
+          const float2 f0 = cmul(cmul(make_float2(t.x, -t.y), lo2(y1)), y2);
+          const float2 f1 = cmul(cmul(make_float2(t.z, -t.w), hi2(y1)), y2);
+          p = pack4(cmul(f0, lo2(p)), cmul(f1, hi2(p)));
+          l = pack4(cmul(f0, lo2(l)), cmul(f1, hi2(l)));
+          psi[base + e] = p;
+          lam[base + e] = l;
+        }
       }
     }
     if (T > 0) {
@@ -161,15 +179,18 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
 #pragma unroll
       for (int j = 0; j < 32; j++) row[j] = F[j];
       const uint64_t fixed = (tile << W) | (static_cast<uint64_t>(tid) << 1);
+      const int ng = static_cast<int>(g.ngen);
 #pragma unroll
       for (int t = 0; t < T; t++) {
-        if (t >= static_cast<int>(g.ngen)) break;
-        const float v = row[g.vm[t]];
-        acc[t] += parity64(fixed & g.fixmask[t]) ? -v : v;
+        const float v = t < ng ? row[g.vm[t]] : 0.0f;
+        accf[t] += parity64(fixed & g.fixmask[t]) ? -v : v;
       }
     }
     __syncthreads();
   }
+  double acc[T > 0 ? T : 1];
+#pragma unroll
+  for (int t = 0; t < (T > 0 ? T : 1); t++) acc[t] = accf[t];
   if constexpr (T > 0) finish<T>(acc, g.ngen, a, out);
 }
 
@@ -305,28 +326,111 @@ struct WarpAdjArgs {
   int8_t arg[kMaxWarpOps];       // lane bit (0..4) or register index
   int8_t gen[kMaxWarpOps];
   int8_t slotidx[kMaxWarpOps];
+  int8_t cls[kMaxWarpOps];       // kMat* structure of m
   M2 m[kMaxWarpOps];
 };
-
-// Im(conj(l_own) (P psi)_own) for one element of a pair; one = the element's
-// wire bit.
-__device__ __forceinline__ float own_term(int gen, float2 p0, float2 p1, float2 l0, float2 l1,
-                                          bool one) {
-  float2 w, l;
-  if (gen == 1) {
-    w = one ? p0 : p1;
-  } else if (gen == 2) {
-    w = one ? make_float2(-p0.y, p0.x) : make_float2(p1.y, -p1.x);
-  } else {
-    w = one ? make_float2(-p1.x, -p1.y) : p0;
-  }
-  l = one ? l1 : l0;
-  return l.x * w.y - l.y * w.x;
-}
 
 __device__ __forceinline__ float4 shfl4(const float4 &v, int mask) {
   return make_float4(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask),
                      __shfl_xor_sync(0xffffffffu, v.z, mask), __shfl_xor_sync(0xffffffffu, v.w, mask));
+}
+
+// Im(conj(l) w) and Re(conj(l) w) summed over both amplitudes of a vector.
+__device__ __forceinline__ float im_dot4(const float4 &l, const float4 &w) {
+  return (l.x * w.y - l.y * w.x) + (l.z * w.w - l.w * w.z);
+}
+__device__ __forceinline__ float re_dot4(const float4 &l, const float4 &w) {
+  return (l.x * w.x + l.y * w.y) + (l.z * w.z + l.w * w.w);
+}
+
+// One op on a lane wire for every register vector. Each lane owns one
+// element of each pair: own' = s own + t other with (s, t) = (a, b) on the
+// wire's 0 side and (d, c) on its 1 side, and it takes its own half of the
+// pair's overlap: X: Im(conj(l) other); Y: -/+ Re(conj(l) other); Z: +/-
+// Im(conj(l) own). A diagonal op needs no partner unless its generator is X
+// or Y (a rotation by zero).
+template <int NV, int CLS>
+__device__ __forceinline__ float lane_op(float4 (&P)[NV], float4 (&L)[NV], int mask, bool one,
+                                         int gen, const M2 &m) {
+  const float2 s = one ? m.d : m.a, t = one ? m.c : m.b;
+  float ov = 0.0f;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    if (CLS == kMatDiag && gen != 1 && gen != 2) {
+      if (gen == 3) ov += im_dot4(L[l], P[l]);
+      P[l] = pack4(cmac2c(CLS, s, lo2(P[l]), t, lo2(P[l])), cmac2c(CLS, s, hi2(P[l]), t, hi2(P[l])));
+      L[l] = pack4(cmac2c(CLS, s, lo2(L[l]), t, lo2(L[l])), cmac2c(CLS, s, hi2(L[l]), t, hi2(L[l])));
+    } else {
+      const float4 Po = shfl4(P[l], mask), Lo = shfl4(L[l], mask);
+      if (gen == 1) ov += im_dot4(L[l], Po);
+      else if (gen == 2) ov += re_dot4(L[l], Po);
+      else if (gen == 3) ov += im_dot4(L[l], P[l]);
+      P[l] = pack4(cmac2c(CLS, s, lo2(P[l]), t, lo2(Po)), cmac2c(CLS, s, hi2(P[l]), t, hi2(Po)));
+      L[l] = pack4(cmac2c(CLS, s, lo2(L[l]), t, lo2(Lo)), cmac2c(CLS, s, hi2(L[l]), t, hi2(Lo)));
+    }
+  }
+  if (gen == 2) return one ? ov : -ov;
+  if (gen == 3) return one ? -ov : ov;
+  return ov;
+}
+
+// One op on wire 0 (the two amplitudes of each vector).
+template <int NV, int CLS>
+__device__ __forceinline__ float wire0_op(float4 (&P)[NV], float4 (&L)[NV], int gen, const M2 &m) {
+  float ov = 0.0f;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    float2 p0 = lo2(P[l]), p1 = hi2(P[l]), l0 = lo2(L[l]), l1 = hi2(L[l]);
+    if (gen) ov += overlap(gen, p0, p1, l0, l1);
+    apply2c(CLS, m, p0, p1);
+    apply2c(CLS, m, l0, l1);
+    P[l] = pack4(p0, p1);
+    L[l] = pack4(l0, l1);
+  }
+  return ov;
+}
+
+// One op on register bit J.
+template <int NV, int J, int CLS>
+__device__ __forceinline__ float reg_op(float4 (&P)[NV], float4 (&L)[NV], int gen, const M2 &m) {
+  float ov = 0.0f;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    if ((l >> J) & 1) continue;
+    const int h = l | (1 << J);
+    float2 pa = lo2(P[l]), pb = lo2(P[h]), qa = hi2(P[l]), qb = hi2(P[h]);
+    float2 la = lo2(L[l]), lb = lo2(L[h]), ma = hi2(L[l]), mb = hi2(L[h]);
+    if (gen) ov += overlap(gen, pa, pb, la, lb) + overlap(gen, qa, qb, ma, mb);
+    apply2c(CLS, m, pa, pb);
+    apply2c(CLS, m, qa, qb);
+    apply2c(CLS, m, la, lb);
+    apply2c(CLS, m, ma, mb);
+    P[l] = pack4(pa, qa);
+    P[h] = pack4(pb, qb);
+    L[l] = pack4(la, ma);
+    L[h] = pack4(lb, mb);
+  }
+  return ov;
+}
+
+template <int NV, int CLS>
+__device__ __forceinline__ float reg_op_any(float4 (&P)[NV], float4 (&L)[NV], int j, int gen,
+                                            const M2 &m) {
+  constexpr int KH = NV == 1 ? 0 : (NV == 2 ? 1 : (NV == 4 ? 2 : (NV == 8 ? 3 : 4)));
+  float ov = 0.0f;
+  if (KH > 0 && j == 0) ov = reg_op<NV, 0, CLS>(P, L, gen, m);
+  if (KH > 1 && j == 1) ov = reg_op<NV, (KH > 1 ? 1 : 0), CLS>(P, L, gen, m);
+  if (KH > 2 && j == 2) ov = reg_op<NV, (KH > 2 ? 2 : 0), CLS>(P, L, gen, m);
+  if (KH > 3 && j == 3) ov = reg_op<NV, (KH > 3 ? 3 : 0), CLS>(P, L, gen, m);
+  return ov;
+}
+
+template <int NV, int CLS>
+__device__ __forceinline__ float warp_op(float4 (&P)[NV], float4 (&L)[NV], int kind, int arg,
+                                         int gen, const M2 &m, uint32_t lane) {
+  if (kind == 0) return wire0_op<NV, CLS>(P, L, gen, m);
+  if (kind == 1) return lane_op<NV, CLS>(P, L, 1 << arg, (lane >> arg) & 1, gen, m);
+  return reg_op_any<NV, CLS>(P, L, arg, gen, m);
 }
 
 template <int KH, int NG>
@@ -338,9 +442,10 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
   const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
-  double acc[NA];
+  // FP32 per thread over its sites (a few dozen at most), FP64 from the warp up.
+  float accf[NA];
 #pragma unroll
-  for (int t = 0; t < NA; t++) acc[t] = 0.0;
+  for (int t = 0; t < NA; t++) accf[t] = 0.0f;
   for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
     uint64_t b = ws;
 #pragma unroll
@@ -356,63 +461,20 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
       P[l] = psi[v];
       L[l] = lam[v];
     }
-    float part[NA];
-#pragma unroll
-    for (int t = 0; t < NA; t++) part[t] = 0.0f;
     for (uint32_t o = 0; o < g.nops; o++) {
       const int kind = g.kind[o], arg = g.arg[o], gen = g.gen[o];
       const M2 m = g.m[o];
-      float ov = 0.0f;
-      if (kind == 0) {
-#pragma unroll
-        for (int l = 0; l < NV; l++) {
-          float2 p0 = lo2(P[l]), p1 = hi2(P[l]), l0 = lo2(L[l]), l1 = hi2(L[l]);
-          if (gen) ov += overlap(gen, p0, p1, l0, l1);
-          apply2(m, p0, p1);
-          apply2(m, l0, l1);
-          P[l] = pack4(p0, p1);
-          L[l] = pack4(l0, l1);
-        }
-      } else if (kind == 1) {
-        const bool one = (lane >> arg) & 1;
-        const float2 c0 = one ? m.c : m.a, c1 = one ? m.d : m.b;
-#pragma unroll
-        for (int l = 0; l < NV; l++) {
-          const float4 Po = shfl4(P[l], 1 << arg), Lo = shfl4(L[l], 1 << arg);
-          const float4 p0 = one ? Po : P[l], p1 = one ? P[l] : Po;
-          const float4 l0 = one ? Lo : L[l], l1 = one ? L[l] : Lo;
-          if (gen)
-            ov += own_term(gen, lo2(p0), lo2(p1), lo2(l0), lo2(l1), one) +
-                  own_term(gen, hi2(p0), hi2(p1), hi2(l0), hi2(l1), one);
-          P[l] = pack4(cmac2(c0, lo2(p0), c1, lo2(p1)), cmac2(c0, hi2(p0), c1, hi2(p1)));
-          L[l] = pack4(cmac2(c0, lo2(l0), c1, lo2(l1)), cmac2(c0, hi2(l0), c1, hi2(l1)));
-        }
-      } else {
-#pragma unroll
-        for (int j = 0; j < KH; j++) {
-          if (j != arg) continue;
-#pragma unroll
-          for (int l = 0; l < NV; l++) {
-            if ((l >> j) & 1) continue;
-            const int h = l | (1 << j);
-            float2 pa = lo2(P[l]), pb = lo2(P[h]), qa = hi2(P[l]), qb = hi2(P[h]);
-            float2 la = lo2(L[l]), lb = lo2(L[h]), ma = hi2(L[l]), mb = hi2(L[h]);
-            if (gen) ov += overlap(gen, pa, pb, la, lb) + overlap(gen, qa, qb, ma, mb);
-            apply2(m, pa, pb);
-            apply2(m, qa, qb);
-            apply2(m, la, lb);
-            apply2(m, ma, mb);
-            P[l] = pack4(pa, qa);
-            P[h] = pack4(pb, qb);
-            L[l] = pack4(la, ma);
-            L[h] = pack4(lb, mb);
-          }
-        }
+      float ov;
+      switch (g.cls[o]) {
+        case kMatReal: ov = warp_op<NV, kMatReal>(P, L, kind, arg, gen, m, lane); break;
+        case kMatRx: ov = warp_op<NV, kMatRx>(P, L, kind, arg, gen, m, lane); break;
+        case kMatDiag: ov = warp_op<NV, kMatDiag>(P, L, kind, arg, gen, m, lane); break;
+        default: ov = warp_op<NV, kMatGeneral>(P, L, kind, arg, gen, m, lane); break;
       }
       if (NG > 0 && gen) {
 #pragma unroll
         for (int t = 0; t < NA; t++)
-          if (t == g.slotidx[o]) part[t] += ov;
+          if (t == g.slotidx[o]) accf[t] += ov;
       }
     }
 #pragma unroll
@@ -424,10 +486,13 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
       psi[v] = P[l];
       lam[v] = L[l];
     }
-#pragma unroll
-    for (int t = 0; t < NA; t++) acc[t] += part[t];
   }
-  if constexpr (NG > 0) finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
+  if constexpr (NG > 0) {
+    double acc[NA];
+#pragma unroll
+    for (int t = 0; t < NA; t++) acc[t] = accf[t];
+    finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
+  }
 }
 
 template <int KH, int NG>
@@ -620,6 +685,7 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
       }
       g.gen[o] = static_cast<int8_t>(gens[o]);
       g.m[o] = m2_from(minv + 8 * o);
+      g.cls[o] = m2_class(g.m[o]);
       g.slotidx[o] = -1;
       if (gens[o]) {
         g.slotidx[o] = static_cast<int8_t>(gi);

@@ -45,6 +45,41 @@ __device__ __forceinline__ void apply2(const M2 &m, float2 &u, float2 &v) {
   v = nv;
 }
 
+// Structure of a 2x2, found on the host: the specialised forms below drop
+// products with exact zeros of the general form (RY-like real matrices,
+// RX-like real diagonal with imaginary off-diagonal, diagonal matrices), so
+// they halve the multiply-adds and round the same way.
+enum : int8_t { kMatGeneral = 0, kMatReal = 1, kMatRx = 2, kMatDiag = 3 };
+
+__host__ inline int8_t m2_class(const M2 &m) {
+  if (m.b.x == 0.0f && m.b.y == 0.0f && m.c.x == 0.0f && m.c.y == 0.0f) return kMatDiag;
+  if (m.a.y == 0.0f && m.b.y == 0.0f && m.c.y == 0.0f && m.d.y == 0.0f) return kMatReal;
+  if (m.a.y == 0.0f && m.d.y == 0.0f && m.b.x == 0.0f && m.c.x == 0.0f) return kMatRx;
+  return kMatGeneral;
+}
+
+// s * own + t * other, where s is the row's own coefficient and t the other
+// one, for a matrix of class cls (t is imaginary for kMatRx, zero for kMatDiag).
+__device__ __forceinline__ float2 cmac2c(int cls, float2 s, float2 own, float2 t, float2 other) {
+  switch (cls) {
+    case kMatReal:
+      return make_float2(s.x * own.x + t.x * other.x, s.x * own.y + t.x * other.y);
+    case kMatRx:
+      return make_float2(s.x * own.x - t.y * other.y, s.x * own.y + t.y * other.x);
+    case kMatDiag:
+      return make_float2(s.x * own.x - s.y * own.y, s.x * own.y + s.y * own.x);
+    default:
+      return cmac2(s, own, t, other);
+  }
+}
+
+__device__ __forceinline__ void apply2c(int cls, const M2 &m, float2 &u, float2 &v) {
+  const float2 nu = cmac2c(cls, m.a, u, m.b, v);
+  const float2 nv = cmac2c(cls, m.d, v, m.c, u);
+  u = nu;
+  v = nv;
+}
+
 __device__ __forceinline__ float2 lo2(const float4 &x) { return make_float2(x.x, x.y); }
 __device__ __forceinline__ float2 hi2(const float4 &x) { return make_float2(x.z, x.w); }
 __device__ __forceinline__ float4 pack4(float2 a, float2 b) {

@@ -58,30 +58,41 @@ def test_tied_parameter_gradients_and_samples():
     out = run_mode(reqs, qm.BATCH_LANES, lanes=3)
     for (inst, gates, terms, shots, seed), (e, g, s) in zip(reqs, out):
         n, edges, p = inst["n"], inst["edges"], len(inst["gammas"])
-        # chain rule over the per-gate entries: RZ(2 gamma) and RX(2 beta)
-        dgamma = np.zeros(p)
-        dbeta = np.zeros(p)
-        k = n                           # after the Hadamard layer
-        for layer in range(p):
-            for _ in edges:
-                dgamma[layer] += 2.0 * g[k + 1]
-                k += 3
-            for _ in range(n):
-                dbeta[layer] += 2.0 * g[k]
-                k += 1
-        assert k == len(gates)
-        eps = 1e-4
-        for layer in range(p):
-            for which, d in (("gammas", dgamma), ("betas", dbeta)):
-                plus = dict(inst); minus = dict(inst)
-                plus[which] = list(inst[which]); minus[which] = list(inst[which])
-                plus[which][layer] += eps
-                minus[which][layer] -= eps
-                ep = oracle.expectation_sum(n, oracle.run(n, W.maxcut_qaoa(
-                    n, edges, plus["gammas"], plus["betas"])), terms)
-                em = oracle.expectation_sum(n, oracle.run(n, W.maxcut_qaoa(
-                    n, edges, minus["gammas"], minus["betas"])), terms)
-                assert abs((ep - em) / (2 * eps) - d[layer]) <= 1e-5
+
+        def tied(grad):
+            """Chain rule over the per-gate entries: RZ(2 gamma), RX(2 beta)."""
+            dgamma, dbeta = np.zeros(p), np.zeros(p)
+            k = n                           # after the Hadamard layer
+            for layer in range(p):
+                for _ in edges:
+                    dgamma[layer] += 2.0 * grad[k + 1]
+                    k += 3
+                for _ in range(n):
+                    dbeta[layer] += 2.0 * grad[k]
+                    k += 1
+            assert k == len(gates)
+            return {"gammas": dgamma, "betas": dbeta}
+
+        got = tied(g)
+        _e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+        want = tied(g0)
+
+        def energy(which, layer, shift):
+            par = {"gammas": list(inst["gammas"]), "betas": list(inst["betas"])}
+            par[which][layer] += shift
+            return oracle.expectation_sum(n, oracle.run(n, W.maxcut_qaoa(
+                n, edges, par["gammas"], par["betas"])), terms)
+
+        h = 1e-3
+        for which in ("gammas", "betas"):
+            for layer in range(p):
+                # the GPU's tied gradient against the oracle's adjoint
+                assert abs(got[which][layer] - want[which][layer]) <= GTOL
+                # and the oracle's chain rule against a fourth-order central
+                # difference of the oracle energy (truncation ~ h^4)
+                fd = (-energy(which, layer, 2 * h) + 8 * energy(which, layer, h)
+                      - 8 * energy(which, layer, -h) + energy(which, layer, -2 * h)) / (12 * h)
+                assert abs(fd - want[which][layer]) <= 1e-6
         # every qubit's marginal within 5 sigma of the exact one
         probs = np.abs(oracle.run(n, gates)) ** 2
         draws = np.array(s, dtype=np.int64)

@@ -394,9 +394,16 @@ def _fused_cases():
     mixed = (W.hea(n, 2, seed=1) + W.random_u3(n, 2, seed=2)
              + [(CCX, (0, 4, 9), ()), (SWAP, (1, 8), ()), (CY, (10, 2), ()), (CZ, (3, 5), ()),
                 (T, (6,), ()), (S, (7,), ())] + W.qaoa_ring_seeded(n, 2, seed=3)[n:])
+    # rotations by zero are identity matrices whose X / Y generators still
+    # need the partner amplitude; H, S, T, SDG mix the other matrix forms
+    zero = [(H, (q,), ()) for q in range(n)] + [(T, (q,), ()) for q in range(0, n, 2)]
+    for q in range(n):
+        zero += [(RX, (q,), (0.0,)), (RY, (q,), (0.0 if q % 2 else 0.8,)), (RZ, (q,), (0.0,)),
+                 (S, (q,), ()), (RX, (q,), (0.3 * q - 1.0,)), (SDG, (q,), ()), (H, (q,), ()),
+                 (RY, (q,), (0.0,))]
     return {"qaoa_ring": W.qaoa_ring_seeded(n, 3, seed=8), "tfim": W.tfim_chain(n, 4),
             "hea_d4": W.hea(n, 4, seed=5), "zz_many": zz_many, "long_wire": long_wire,
-            "mixed": mixed}
+            "mixed": mixed, "zero_angles": zero}
 
 
 @pytest.mark.parametrize("name", list(_fused_cases()))
