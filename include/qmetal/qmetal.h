@@ -34,7 +34,12 @@ typedef enum {
   QM_RX = 8, QM_RY = 9, QM_RZ = 10, QM_P = 11,
   QM_CX = 12, QM_CY = 13, QM_CZ = 14, QM_SWAP = 15,
   QM_CP = 16,
-  QM_CCX = 17
+  QM_CCX = 17,
+  /* Appended here (the reference stops at QM_CCX): U3(theta, phi, lambda) =
+   * [[cos(theta/2), -e^{i lambda} sin(theta/2)],
+   *  [e^{i phi} sin(theta/2), e^{i(phi + lambda)} cos(theta/2)]],
+   * one qubit and exactly three parameters; not differentiable. */
+  QM_U3 = 18
 } qm_gate_kind;
 
 typedef struct qm_simulator_s *qm_simulator;

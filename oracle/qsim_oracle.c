@@ -20,7 +20,8 @@
  *
  * Conventions: LSB-first (qubit q is bit q of the basis index); states are
  * complex128 stored interleaved (re, im). Gate kinds use the qm_gate_kind
- * numbering of the C ABI (X=0 ... CCX=17).
+ * numbering of the C ABI (X=0 ... CCX=17, and U3=18, which the library
+ * appends to the ABI: its matrix is the OpenQASM U(theta, phi, lambda)).
  *
  * Plan ops arrive in the flat serialisation produced by the library's plan
  * builder (and by the reference shim): see qo_run_plan for the layout.
@@ -44,7 +45,7 @@ typedef double _Complex cplx;
 enum {
   K_X = 0, K_Y, K_Z, K_H, K_S, K_SDG, K_T, K_TDG,
   K_RX, K_RY, K_RZ, K_P,
-  K_CX, K_CY, K_CZ, K_SWAP, K_CP, K_CCX
+  K_CX, K_CY, K_CZ, K_SWAP, K_CP, K_CCX, K_U3
 };
 
 /* Plan-op kinds, in the order of PlanOp::Kind (include/qmetal/plan.h:27-35). */
@@ -85,6 +86,11 @@ static int gate_matrix(int kind, const double *p, cplx m[4]) {
     case K_P:
       m[0] = 1; m[1] = 0; m[2] = 0; m[3] = polar1(p[0]);
       return 0;
+    case K_U3: {
+      double c = cos(p[0] / 2), s = sin(p[0] / 2);
+      m[0] = c; m[1] = -s * polar1(p[2]); m[2] = s * polar1(p[1]); m[3] = c * polar1(p[1] + p[2]);
+      return 0;
+    }
     default:
       return -1;
   }

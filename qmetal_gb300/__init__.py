@@ -153,6 +153,7 @@ def _check(rc: int) -> None:
 X, Y, Z, H, S, SDG, T, TDG = range(8)
 RX, RY, RZ, P = 8, 9, 10, 11
 CX, CY, CZ, SWAP, CP, CCX = 12, 13, 14, 15, 16, 17
+U3 = 18   # appended to the ABI: U3(theta, phi, lambda), not differentiable
 
 
 def version() -> tuple[int, int, int]:
@@ -260,6 +261,7 @@ class Circuit:
     def ry(self, q, theta): return self._add(RY, (q,), (theta,))
     def rz(self, q, theta): return self._add(RZ, (q,), (theta,))
     def p(self, q, theta): return self._add(P, (q,), (theta,))
+    def u3(self, q, theta, phi, lam): return self._add(U3, (q,), (theta, phi, lam))
 
     # multi-qubit
     def cx(self, c, t): return self._add(CX, (c, t))

@@ -45,9 +45,9 @@ int guarded(Fn &&fn) {
 }
 
 GateKind kind_of(int k) {
-  if (k < QM_X || k > QM_CCX) throw std::runtime_error("unknown gate code");
-  static const GateKind map[] = {G_X, G_Y, G_Z, G_H, G_S, G_SDG, G_T, G_TDG, G_RX,
-                                 G_RY, G_RZ, G_P, G_CX, G_CY, G_CZ, G_SWAP, G_CP, G_CCX};
+  if (k < QM_X || k > QM_U3) throw std::runtime_error("unknown gate code");
+  static const GateKind map[] = {G_X,  G_Y,  G_Z,  G_H,  G_S,  G_SDG, G_T,    G_TDG, G_RX, G_RY,
+                                 G_RZ, G_P,  G_CX, G_CY, G_CZ, G_SWAP, G_CP, G_CCX, G_U3};
   return map[k];
 }
 
@@ -75,6 +75,8 @@ Gate gate_of(uint32_t width, qm_gate_kind kind, const uint32_t *qubits, uint32_t
   if (np && !params) throw std::runtime_error("null parameter array");
   Gate g{};
   g.kind = kind_of(kind);
+  if (g.kind == G_U3 && (nq != 1 || np != 3))
+    throw std::runtime_error("u3 takes one qubit and three parameters");
   g.num_qubits = static_cast<uint8_t>(nq);
   g.num_params = static_cast<uint8_t>(np);
   for (uint32_t i = 0; i < nq; i++) {

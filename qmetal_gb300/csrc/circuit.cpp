@@ -23,7 +23,7 @@ Gate g3(GateKind k, uint32_t a, uint32_t b, uint32_t c) {
 const char *gate_name(GateKind k) {
   static const char *names[G_KIND_COUNT] = {
       "x", "y", "z", "h", "s", "sdg", "t", "tdg", "rx", "ry", "rz", "p",
-      "cx", "cy", "cz", "swap", "cp", "ccx"};
+      "cx", "cy", "cz", "swap", "cp", "ccx", "u3"};
   return (k < G_KIND_COUNT) ? names[k] : "?";
 }
 
@@ -58,6 +58,15 @@ void gate_matrix_1q(GateKind k, const double *p, cdouble m[4]) {
     case G_P:
       m[0] = 1.0; m[1] = 0.0; m[2] = 0.0; m[3] = std::polar(1.0, p[0]);
       return;
+    case G_U3: {
+      // The appended gate; the OpenQASM definition of U(theta, phi, lambda).
+      const double c = std::cos(p[0] / 2), s = std::sin(p[0] / 2);
+      m[0] = c;
+      m[1] = -std::polar(s, p[2]);
+      m[2] = std::polar(s, p[1]);
+      m[3] = std::polar(c, p[1] + p[2]);
+      return;
+    }
     default:
       throw std::runtime_error("gate_matrix_1q: not a 1-qubit gate");
   }

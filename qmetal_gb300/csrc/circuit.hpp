@@ -24,6 +24,7 @@ enum GateKind : uint8_t {
   G_CX, G_CY, G_CZ, G_SWAP,
   G_CP,
   G_CCX,
+  G_U3,            // appended: not in the reference's GateKind
   G_KIND_COUNT
 };
 

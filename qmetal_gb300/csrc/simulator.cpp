@@ -61,6 +61,11 @@ Gate invert(const Gate &g) {
     case G_SDG: inv.kind = G_S; break;
     case G_T: inv.kind = G_TDG; break;
     case G_TDG: inv.kind = G_T; break;
+    case G_U3:   // U3(t, f, l)^-1 = U3(-t, -l, -f)
+      inv.params[0] = -g.params[0];
+      inv.params[1] = -g.params[2];
+      inv.params[2] = -g.params[1];
+      break;
     default: break;
   }
   return inv;

@@ -460,3 +460,26 @@ def test_gradient_matches_oracle_adjoint_wide():
     e, g = qm.Simulator(n).energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
     assert abs(e - e0) <= 1e-5
     assert np.abs(np.array(g) - g0).max() <= 1e-5
+
+
+@pytest.mark.parametrize("mode", ["fused", "unfused", "gates"])
+def test_u3_every_wire(mode):
+    """The appended U3 gate (kind 18) on every wire of a 12-qubit state,
+    alone and in fused windows with CX / CZ layers."""
+    U3 = qm.U3
+    n = 12
+    rng = np.random.default_rng(31)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    gates = []
+    for layer in range(3):
+        for q in range(n):
+            gates.append((U3, (q,), tuple(float(x) for x in rng.uniform(-3.1, 3.1, 3))))
+        for q in range(layer % 2, n - 1, 2):
+            gates.append((CX if layer % 2 else CZ, (q, q + 1), ()))
+    d, sim = compare(n, gates, mode, init)
+    assert d <= 1e-5
+    assert abs(sim.norm() - 1) <= 1e-5
+    # U3 carries parameters without a native generator: the gradient fails closed
+    with pytest.raises(qm.QMetalError, match="differentiable"):
+        sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian([(1.0, 0, 0, 1)]))
