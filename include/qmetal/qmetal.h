@@ -129,6 +129,14 @@ int qm_apply_gate(qm_simulator s, qm_gate_kind kind, const uint32_t *qubits,
  * src/metal/simulator.mm:189-196 and 436-448). */
 int qm_run_cached(qm_simulator s, qm_circuit c);
 
+/* qm_run with the executor's own merging on top of the default plan: a
+ * window's one-qubit ops packed into passes of up to ten wires, and runs of
+ * CX / SWAP ops applied as one GF(2)-affine permutation pass where that moves
+ * fewer bytes (it needs a second state-sized buffer, taken on first use while
+ * the device has room; otherwise the ops run one by one). Same unitary as
+ * qm_run; the reference has no counterpart. */
+int qm_run_merged(qm_simulator s, qm_circuit c);
+
 /* Run with explicit fusion options (FusionOptions, reference plan.h:76-94). */
 int qm_run_options(qm_simulator s, qm_circuit c, int collapse_1q_windows,
                    int fuse_diagonals, int recognize_zz, uint32_t group_1q,

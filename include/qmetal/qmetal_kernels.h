@@ -65,6 +65,17 @@ int qmk_apply_controlled(float *state, uint32_t n, uint32_t num_controls,
 int qmk_apply_swap(float *state, uint32_t n, uint32_t a, uint32_t b,
                    void *stream);
 
+/* A basis permutation affine over GF(2), out of place: dst[y] = src[G(y)]
+ * with G(y) = offset ^ XOR of cols[j] over the set bits j of y (cols[j] is
+ * the image of bit j; n entries, each non-zero and inside n bits, jointly
+ * invertible). A run of CX / SWAP / X gates is such a map, so the run costs
+ * one pass instead of one per gate; it replaces consecutive
+ * apply_controlled_1q / apply_swap dispatches (simulator.mm:526-547) and has
+ * no single counterpart there. dst and src must not overlap. Returns -1 for
+ * a singular map or bad arguments, without launching. */
+int qmk_apply_permutation(float *dst, const float *src, uint32_t n,
+                          const uint64_t *cols, uint64_t offset, void *stream);
+
 /* Scratch bytes every workspace must hold for a simulator of n qubits (the
  * diagonal-layer tables and reduction partials). */
 size_t qmk_workspace_bytes(uint32_t n);

@@ -102,6 +102,7 @@ _reset = _decl("qm_reset", c_int, c_void_p)
 _run = _decl("qm_run", c_int, c_void_p, c_void_p)
 _run_unfused = _decl("qm_run_unfused", c_int, c_void_p, c_void_p)
 _run_cached = _decl("qm_run_cached", c_int, c_void_p, c_void_p)
+_run_merged = _decl("qm_run_merged", c_int, c_void_p, c_void_p)
 _run_options = _decl("qm_run_options", c_int, c_void_p, c_void_p, c_int, c_int,
                      c_int, c_uint32, c_uint32)
 _sync = _decl("qm_synchronize", c_int, c_void_p)
@@ -316,6 +317,12 @@ class Simulator:
 
     def run(self, circuit: Circuit, fuse: bool = True):
         _check((_run if fuse else _run_unfused)(self._h, circuit._h))
+        return self
+
+    def run_merged(self, circuit: Circuit):
+        """run() with the executor's merging on top of the plan: wider
+        one-qubit passes and CX / SWAP runs as one permutation pass."""
+        _check(_run_merged(self._h, circuit._h))
         return self
 
     def run_cached(self, circuit: Circuit):

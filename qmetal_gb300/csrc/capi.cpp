@@ -225,6 +225,14 @@ int qm_run_cached(qm_simulator s, qm_circuit c) {
   return guarded([&] { s->s->run_cached(c->c); });
 }
 
+int qm_run_merged(qm_simulator s, qm_circuit c) {
+  if (!s || !c) {
+    set_error("null argument");
+    return -1;
+  }
+  return guarded([&] { s->s->run_merged(c->c); });
+}
+
 int qm_run_unfused(qm_simulator s, qm_circuit c) {
   if (!s || !c) {
     set_error("null argument");

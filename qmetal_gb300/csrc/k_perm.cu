@@ -1,0 +1,130 @@
+// k_perm.cu -- basis permutations that are affine over GF(2) (runs of CX and
+// SWAP gates) applied in one out-of-place gather pass.
+//
+// A CX flips bit t of the basis index where bit c is set, a SWAP exchanges
+// two bits, an X flips one: each maps index x to A x ^ b with A invertible
+// over GF(2), and so does any run of them. The reference applies such a run
+// one gate at a time (Controlled1q / Swap plan ops, src/metal/simulator.mm:
+// 526-558, one pass over half or all of the state per gate); here the whole
+// run is one gather, dst[y] = src[G(y)] with G(y) = off ^ XOR_{j : y_j = 1}
+// col_j, i.e. 2S of traffic however many gates the run holds. Writes are
+// whole 512-byte warp stores; reads follow G, which for the runs the executor
+// fuses keeps a warp's sources within a few 32-byte sectors.
+#include <cstdint>
+#include <vector>
+
+#include "kcommon.cuh"
+#include "../../include/qmetal/qmetal_kernels.h"
+
+using namespace qmk;
+using qmk_host::launch_status;
+
+namespace {
+
+constexpr int kTileBits = 13;     // amplitude bits resolved by the shared tables
+constexpr int kMaxBits = 40;
+
+struct PermArgs {
+  uint64_t off;                   // G(0)
+  uint64_t lo[kTileBits];         // images of amplitude bits 0..12
+  uint64_t hi[kMaxBits - kTileBits];
+  uint32_t n;
+  uint32_t pair;                  // 1: G maps bit 0 to bit 0 only
+};
+
+__global__ void __launch_bounds__(kThreads)
+k_permute(float4 *__restrict__ dst, const float2 *__restrict__ src, uint64_t ntiles, PermArgs a) {
+  __shared__ uint64_t T0[128], T1[64];     // XOR sums of lo[0..6], lo[7..12]
+  const uint32_t tid = threadIdx.x;
+  for (uint32_t i = tid; i < 128; i += kThreads) {
+    uint64_t v = 0;
+    for (int j = 0; j < 7; j++)
+      if ((i >> j) & 1) v ^= a.lo[j];
+    T0[i] = v;
+  }
+  for (uint32_t i = tid; i < 64; i += kThreads) {
+    uint64_t v = 0;
+    for (int j = 0; j < 6; j++)
+      if ((i >> j) & 1) v ^= a.lo[7 + j];
+    T1[i] = v;
+  }
+  __syncthreads();
+  const uint32_t W = a.n < kTileBits ? a.n : kTileBits;
+  const uint32_t nv = 1u << (W - 1);                // vectors per tile
+  const float4 *src4 = reinterpret_cast<const float4 *>(src);
+  constexpr int UU = 8;
+  for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    uint64_t H = a.off;
+    for (uint32_t b = 0; b + W < a.n; b++)
+      if ((tile >> b) & 1) H ^= a.hi[b];
+    for (uint32_t e0 = tid; e0 < nv; e0 += kThreads * UU) {
+      float4 r[UU];
+#pragma unroll
+      for (int u = 0; u < UU; u++) {
+        const uint32_t e = e0 + u * kThreads;
+        if (e >= nv) continue;
+        const uint32_t y = 2 * e;
+        const uint64_t x0 = H ^ T0[y & 127] ^ T1[(y >> 7) & 63];
+        if (a.pair) {
+          const float4 v = __ldg(&src4[x0 >> 1]);
+          r[u] = (x0 & 1) ? make_float4(v.z, v.w, v.x, v.y) : v;
+        } else {
+          const float2 p = __ldg(&src[x0]), q = __ldg(&src[x0 ^ a.lo[0]]);
+          r[u] = make_float4(p.x, p.y, q.x, q.y);
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < UU; u++) {
+        const uint32_t e = e0 + u * kThreads;
+        if (e < nv) dst[tile * nv + e] = r[u];
+      }
+    }
+  }
+}
+
+// Rank of the columns over GF(2): the map is a bijection iff rank == n.
+uint32_t gf2_rank(const uint64_t *cols, uint32_t n) {
+  std::vector<uint64_t> v(cols, cols + n);
+  uint32_t rank = 0;
+  for (uint32_t bit = 0; bit < n && rank < n; bit++) {
+    const uint64_t m = 1ull << bit;
+    uint32_t piv = rank;
+    while (piv < n && !(v[piv] & m)) piv++;
+    if (piv == n) continue;
+    std::swap(v[rank], v[piv]);
+    for (uint32_t r = 0; r < n; r++)
+      if (r != rank && (v[r] & m)) v[r] ^= v[rank];
+    rank++;
+  }
+  return rank;
+}
+
+}  // namespace
+
+extern "C" int qmk_apply_permutation(float *dst, const float *src, uint32_t n,
+                                     const uint64_t *cols, uint64_t offset, void *stream) {
+  if (!dst || !src || !cols || n < 1 || n > kMaxBits) return -1;
+  if ((reinterpret_cast<uintptr_t>(dst) & 15u) || (reinterpret_cast<uintptr_t>(src) & 15u))
+    return -1;
+  if (dst == src) return -1;                        // out of place only
+  const uint64_t all = (n >= 64) ? ~0ull : ((1ull << n) - 1);
+  if (offset & ~all) return -1;
+  for (uint32_t j = 0; j < n; j++)
+    if (!cols[j] || (cols[j] & ~all)) return -1;
+  if (gf2_rank(cols, n) != n) return -1;            // not a bijection
+  PermArgs a{};
+  a.off = offset;
+  a.n = n;
+  for (uint32_t j = 0; j < n; j++) {
+    if (j < kTileBits) a.lo[j] = cols[j];
+    else a.hi[j - kTileBits] = cols[j];
+  }
+  a.pair = cols[0] == 1ull ? 1u : 0u;
+  const uint32_t W = n < kTileBits ? n : kTileBits;
+  const uint64_t ntiles = 1ull << (n - W);
+  const uint64_t cap = static_cast<uint64_t>(qmk_host::num_sms()) * 8;
+  const unsigned grid = static_cast<unsigned>(ntiles < cap ? ntiles : cap);
+  k_permute<<<grid, kThreads, 0, (cudaStream_t)stream>>>(
+      reinterpret_cast<float4 *>(dst), reinterpret_cast<const float2 *>(src), ntiles, a);
+  return launch_status();
+}

@@ -83,6 +83,71 @@ int generator_of(const Gate &g) {
 
 uint32_t popc(uint64_t x) { return static_cast<uint32_t>(__builtin_popcountll(x)); }
 
+// x -> A x ^ off over GF(2); cols[j] = A e_j.
+struct Affine {
+  std::vector<uint64_t> cols;
+  uint64_t off = 0;
+  explicit Affine(uint32_t n) : cols(n) {
+    for (uint32_t j = 0; j < n; j++) cols[j] = 1ull << j;
+  }
+  // Compose g after the map: x -> g(A x ^ off), g a CX (c, t) or a SWAP (a, b).
+  void then_cx(uint32_t c, uint32_t t) {
+    auto f = [&](uint64_t v) { return v ^ (((v >> c) & 1ull) << t); };
+    for (uint64_t &v : cols) v = f(v);
+    off = f(off);
+  }
+  void then_swap(uint32_t a, uint32_t b) {
+    auto f = [&](uint64_t v) {
+      const uint64_t d = ((v >> a) ^ (v >> b)) & 1ull;
+      return v ^ (d << a) ^ (d << b);
+    };
+    for (uint64_t &v : cols) v = f(v);
+    off = f(off);
+  }
+  // Distinct 32-byte sectors a warp's 64 sources touch (16 when contiguous).
+  uint32_t sectors() const {
+    std::vector<uint64_t> s;
+    for (uint64_t y = 0; y < 64 && y < (1ull << cols.size()); y++) {
+      uint64_t x = off;
+      for (uint32_t j = 0; j < cols.size() && j < 6; j++)
+        if ((y >> j) & 1) x ^= cols[j];
+      s.push_back(x >> 2);
+    }
+    std::sort(s.begin(), s.end());
+    return static_cast<uint32_t>(std::unique(s.begin(), s.end()) - s.begin());
+  }
+};
+
+// One gate of a permutation run: CX (control, target) or SWAP (a, b).
+struct PermGate {
+  bool swap;
+  uint32_t a, b;
+};
+
+// Gather map for a run applied forward (x -> F(x), so dst[y] = src[F^-1(y)])
+// or undone (dst[y] = src[F(y)]); every gate of the run is an involution.
+Affine run_map(uint32_t n, const std::vector<PermGate> &run, bool undo) {
+  Affine m(n);
+  auto step = [&](const PermGate &g) {
+    if (g.swap) m.then_swap(g.a, g.b);
+    else m.then_cx(g.a, g.b);
+  };
+  if (undo) {
+    for (const PermGate &g : run) step(g);
+  } else {
+    for (size_t k = run.size(); k-- > 0;) step(run[k]);
+  }
+  return m;
+}
+
+// A gather pass moves 2S, more when the warp's sources scatter; the run's
+// gates move S each (half the state read and written per CX, all of it
+// crossing for a SWAP, counted as S by the roofline model).
+bool permutation_pays(const Affine &m, size_t gates) {
+  const double pass = 2.0 * std::max(1.0, m.sectors() / 16.0);
+  return pass * 1.25 < static_cast<double>(gates);
+}
+
 struct FlipGroup {
   uint64_t flip;
   std::vector<size_t> terms;
@@ -183,6 +248,8 @@ void Simulator::release() {
   graphs_.clear();
   cudaFree(state_);
   cudaFree(costate_);
+  cudaFree(scratch_);
+  scratch_ = nullptr;
   cudaFree(ws_);
   cudaFree(sample_ws_);
   cudaFree(d_shots_);
@@ -221,6 +288,37 @@ void Simulator::reset() {
 void Simulator::synchronize() {
   activate();
   cuda_check(cudaStreamSynchronize(S(stream_)), "GPU error");
+}
+
+bool Simulator::ensure_scratch() {
+  if (scratch_) return true;
+  if (scratch_failed_) return false;
+  const size_t bytes = dim() * 8;
+  size_t free_b = 0, total_b = 0;
+  // Keep 2 GiB of headroom for other simulators and the runtime.
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < bytes + (2ull << 30) ||
+      cudaMalloc(&scratch_, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    scratch_ = nullptr;
+    scratch_failed_ = true;
+    return false;
+  }
+  return true;
+}
+
+void Simulator::invalidate_graphs() {
+  for (const GraphEntry &e : graphs_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(e.exec));
+  graphs_.clear();
+}
+
+bool Simulator::permute(float *&buf, const std::vector<uint64_t> &cols, uint64_t off) {
+  if (!ensure_scratch()) return false;
+  check(qmk_apply_permutation(scratch_, buf, n_, cols.data(), off, stream_), "permutation");
+  dispatches_++;
+  std::swap(buf, scratch_);
+  // Captured graphs hold the old state pointer.
+  invalidate_graphs();
+  return true;
 }
 
 // ---------------------------------------------------------------------------
@@ -417,7 +515,33 @@ void Simulator::run_merged(const Plan &p) {
     wires.clear();
     mats.clear();
   };
+  // Consecutive CX / SWAP ops: one permutation pass when that moves fewer
+  // bytes than the ops one by one.
+  std::vector<PermGate> run;
+  std::vector<const PlanOp *> run_ops;
+  auto flush_run = [&]() {
+    if (run.empty()) return;
+    bool done = false;
+    if (run.size() >= 2) {
+      const Affine map = run_map(n_, run, false);
+      if (permutation_pays(map, run.size())) done = permute(state_, map.cols, map.off);
+    }
+    if (!done)
+      for (const PlanOp *o : run_ops) apply_op_to(state_, *o);
+    run.clear();
+    run_ops.clear();
+  };
   for (const PlanOp &op : p.ops) {
+    const bool cx = op.kind == PlanOp::Kind::Controlled1q && op.matrix[0] == 0.0 &&
+                    op.matrix[1] == 1.0 && op.matrix[2] == 1.0 && op.matrix[3] == 0.0;
+    if ((cx || op.kind == PlanOp::Kind::Swap) && op.qubits[0] < n_ && op.qubits[1] < n_ &&
+        op.qubits[0] != op.qubits[1]) {
+      flush();
+      run.push_back({op.kind == PlanOp::Kind::Swap, op.qubits[0], op.qubits[1]});
+      run_ops.push_back(&op);
+      continue;
+    }
+    flush_run();
     std::vector<uint32_t> w;
     std::vector<cdouble> m;
     if (op.kind == PlanOp::Kind::Dense1q) {
@@ -451,6 +575,12 @@ void Simulator::run_merged(const Plan &p) {
     }
   }
   flush();
+  flush_run();
+}
+
+void Simulator::run_merged(const Circuit &c) {
+  if (c.num_qubits != n_) throw std::runtime_error("circuit/simulator size mismatch");
+  run_merged(build_plan(c, FusionOptions{}));
 }
 
 void Simulator::run_profiled(const Plan &p, std::vector<double> &seconds) {
@@ -940,6 +1070,31 @@ void Simulator::sweep_fused(const Circuit &c) {
     const Segment &seg = segs[s];
     const bool undo = s > first;
     if (seg.kind == Segment::Single) {
+      // A run of CX / SWAP gates, all undone here, goes as one permutation
+      // pass per state when that moves fewer bytes.
+      auto perm_gate = [&](size_t k) {
+        const Gate &g = c.ops[segs[k].begin];
+        return segs[k].kind == Segment::Single && (g.kind == G_CX || g.kind == G_SWAP) &&
+               g.qubits[0] < n_ && g.qubits[1] < n_ && g.qubits[0] != g.qubits[1];
+      };
+      if (undo && perm_gate(s)) {
+        size_t lo = s;
+        while (lo - 1 > first && perm_gate(lo - 1)) lo--;
+        if (s > lo) {
+          std::vector<PermGate> run;
+          for (size_t k = lo; k <= s; k++) {
+            const Gate &g = c.ops[segs[k].begin];
+            run.push_back({g.kind == G_SWAP, g.qubits[0], g.qubits[1]});
+          }
+          const Affine map = run_map(n_, run, true);
+          if (permutation_pays(map, run.size()) && permute(state_, map.cols, map.off)) {
+            if (!permute(costate_, map.cols, map.off))
+              throw std::runtime_error("permutation: scratch buffer lost");
+            s = lo;
+            continue;
+          }
+        }
+      }
       if (undo) {
         const Gate inv = invert(c.ops[seg.begin]);
         apply_gate_to(state_, inv);

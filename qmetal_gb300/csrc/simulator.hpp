@@ -36,8 +36,10 @@ class Simulator {
   // replay the graph with one launch. Same kernels, same results.
   void run_cached(const Circuit &c);
   // The plan with each window's consecutive one-qubit ops merged into as few
-  // group passes as the tile allows (same unitary, fewer passes).
+  // group passes as the tile allows, and runs of CX / SWAP ops applied as one
+  // permutation pass where that moves fewer bytes (same unitary, fewer passes).
   void run_merged(const Plan &p);
+  void run_merged(const Circuit &c);
   // Runs the plan with a CUDA event between ops; seconds[i] = op i's device time.
   void run_profiled(const Plan &p, std::vector<double> &seconds);
   void synchronize();
@@ -97,12 +99,21 @@ class Simulator {
   void sweep_fused(const Circuit &c);
   void fetch(size_t count);             // d_results_ -> h_results_, sync
   void launch_sample(size_t shots, uint64_t seed);
+  // Out-of-place permutation passes need a second state-sized buffer; it is
+  // allocated on first use, and only while the device has room for it.
+  bool ensure_scratch();
+  // buf <- buf gathered through the affine map (cols, off); buf then names
+  // the gathered buffer and the old one becomes the scratch.
+  bool permute(float *&buf, const std::vector<uint64_t> &cols, uint64_t off);
+  void invalidate_graphs();
 
   uint32_t n_ = 0;
   int device_ = 0;
   void *stream_ = nullptr;
   float *state_ = nullptr;
   float *costate_ = nullptr;
+  float *scratch_ = nullptr;
+  bool scratch_failed_ = false;
   void *ws_ = nullptr;
   size_t ws_bytes_ = 0;
   void *sample_ws_ = nullptr;
