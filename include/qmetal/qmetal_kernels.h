@@ -130,6 +130,18 @@ int qmk_pauli_accum(float *lambda, const float *psi, uint32_t n,
                     const uint64_t *sign_masks, const uint32_t *ny,
                     const double *coeffs, int overwrite, void *stream);
 
+/* lambda (=|+=) sum_t coeff_t * i^ny_t * P_t psi for terms that each flip a
+ * single wire (wires[t]; sign mask and Y count as for qmk_pauli_accum), up
+ * to 16 per call, on wire 0, wires 1..5 and at most four wires >= 6, with
+ * n >= 6 + that count: one pass over both states for all of them, where the
+ * per-flip form takes one pass per wire (a transverse field on n wires is
+ * n passes there). No counterpart in the reference, which builds the
+ * co-state one term per pass (simulator.mm:856-895). */
+int qmk_pauli_accum_local(float *lambda, const float *psi, uint32_t n,
+                          uint32_t num_terms, const uint32_t *wires,
+                          const uint64_t *sign_masks, const uint32_t *ny,
+                          const double *coeffs, int overwrite, void *stream);
+
 /* Re<a|b> into *d_out. Replaces the host energy loop of simulator.mm:897-904. */
 int qmk_dot_re(const float *a, const float *b, uint32_t n, double *d_out,
                void *workspace, size_t workspace_bytes, void *stream);

@@ -330,10 +330,6 @@ struct WarpAdjArgs {
   M2 m[kMaxWarpOps];
 };
 
-__device__ __forceinline__ float4 shfl4(const float4 &v, int mask) {
-  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask),
-                     __shfl_xor_sync(0xffffffffu, v.z, mask), __shfl_xor_sync(0xffffffffu, v.w, mask));
-}
 
 // Im(conj(l) w) and Re(conj(l) w) summed over both amplitudes of a vector.
 __device__ __forceinline__ float im_dot4(const float4 &l, const float4 &w) {

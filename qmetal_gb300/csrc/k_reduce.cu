@@ -7,6 +7,7 @@
 // block order, so a result depends only on the grid size, never on timing.
 #include <algorithm>
 #include <cstring>
+#include <vector>
 
 #include "kreduce.cuh"
 #include "../../include/qmetal/qmetal_kernels.h"
@@ -260,6 +261,98 @@ bool ok_ws(void *ws, size_t bytes, uint32_t n) {
   return ws && bytes >= qmk_workspace_bytes(n);
 }
 
+// ---------------------------------------------------------------------------
+// Co-state terms that each flip a single wire (a transverse field, X_a Z_b
+// ...), many wires per pass. A warp owns 32 consecutive vectors (lane =
+// vector bits 0..4, i.e. wires 1..5) for every combination of up to KH wires
+// >= 6 held in registers; the flipped source of an output amplitude is the
+// other half of its vector (wire 0), the partner lane's vector (wires 1..5)
+// or another register (wires >= 6), so psi is read once for all the terms.
+
+constexpr int kLocalTerms = 16;
+
+struct LocalAccumArgs {
+  uint32_t nt;
+  uint32_t hpos[4];               // wires >= 6 of the tile: vector bit - 5
+  int8_t kind[kLocalTerms];       // 0: wire 0, 1: lane bit, 2: register bit
+  int8_t arg[kLocalTerms];        // lane bit or register index
+  uint64_t sign[kLocalTerms];     // sign mask at the source index
+  uint32_t lpar[kLocalTerms];     // bit l: parity of the register bits of vector l & sign
+  uint32_t fpar;                  // bit t: parity(flip_t & sign_t)
+  float2 kappa[kLocalTerms];      // coeff * i^ny
+};
+
+template <int NV, int J>
+__device__ __forceinline__ float4 reg_source(const float4 (&P)[NV], int l) {
+  float4 r = P[0];
+#pragma unroll
+  for (int k = 0; k < NV; k++)
+    if (k == (l ^ (1 << J))) r = P[k];
+  return r;
+}
+
+template <int KH, bool OVERWRITE>
+__global__ void __launch_bounds__(kThreads)
+k_accum_local(float4 *__restrict__ lam, const float4 *__restrict__ psi, uint64_t nwsites,
+              LocalAccumArgs c) {
+  constexpr int NV = 1 << KH;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
+  for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
+    uint64_t b = ws;
+#pragma unroll
+    for (int j = 0; j < KH; j++) b = ins0(b, c.hpos[j]);
+    const uint64_t base = (b << 5) | lane;
+    auto vec_of = [&](int l) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (c.hpos[j] + 5);
+      return v;
+    };
+    float4 P[NV], L[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      const uint64_t v = vec_of(l);
+      P[l] = psi[v];
+      L[l] = OVERWRITE ? make_float4(0.f, 0.f, 0.f, 0.f) : lam[v];
+    }
+    for (uint32_t t = 0; t < c.nt; t++) {
+      const int kind = c.kind[t], arg = c.arg[t];
+      const uint64_t sg = c.sign[t];
+      // parity of (output index ^ flip) & sign, for amplitude 0 of vector l:
+      // the site's bits, the register bits of l, and the flip's own bits.
+      const uint32_t p0 = parity64((base << 1) & sg) ^ ((c.fpar >> t) & 1u);
+      const uint32_t p1 = p0 ^ static_cast<uint32_t>(sg & 1ull);
+      const float2 k = c.kappa[t];
+      const uint32_t lpar = c.lpar[t];
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        float4 q;
+        if (kind == 0) {
+          q = make_float4(P[l].z, P[l].w, P[l].x, P[l].y);
+        } else if (kind == 1) {
+          q = shfl4(P[l], 1 << arg);
+        } else {
+          q = P[l];
+          if (KH > 0 && arg == 0) q = reg_source<NV, 0>(P, l);
+          if (KH > 1 && arg == 1) q = reg_source<NV, (KH > 1 ? 1 : 0)>(P, l);
+          if (KH > 2 && arg == 2) q = reg_source<NV, (KH > 2 ? 2 : 0)>(P, l);
+          if (KH > 3 && arg == 3) q = reg_source<NV, (KH > 3 ? 3 : 0)>(P, l);
+        }
+        const uint32_t lp = (lpar >> l) & 1u;
+        const float2 k0 = (p0 ^ lp) ? make_float2(-k.x, -k.y) : k;
+        const float2 k1 = (p1 ^ lp) ? make_float2(-k.x, -k.y) : k;
+        const float2 a = cmul(k0, lo2(q)), d = cmul(k1, hi2(q));
+        L[l] = make_float4(L[l].x + a.x, L[l].y + a.y, L[l].z + d.x, L[l].w + d.y);
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < NV; l++) lam[vec_of(l)] = L[l];
+  }
+}
+
 }  // namespace
 
 extern "C" int qmk_abs2sum(const float *state, uint32_t n, double *d_out,
@@ -331,6 +424,73 @@ extern "C" int qmk_pauli_accum(float *lam, const float *psi, uint32_t n, uint64_
   else if (nt <= 4) launch_accum<4>(lam, psi, n, c, ow, s);
   else if (nt <= 8) launch_accum<8>(lam, psi, n, c, ow, s);
   else launch_accum<16>(lam, psi, n, c, ow, s);
+  return launch_status();
+}
+
+extern "C" int qmk_pauli_accum_local(float *lam, const float *psi, uint32_t n, uint32_t nt,
+                                     const uint32_t *wires, const uint64_t *signs,
+                                     const uint32_t *ny, const double *coeffs, int overwrite,
+                                     void *stream) {
+  if (!lam || !psi || n < 6 || n > 40 || nt < 1 || nt > kLocalTerms || !wires || !signs || !ny ||
+      !coeffs)
+    return -1;
+  const uint64_t all = (1ull << n) - 1;
+  std::vector<uint32_t> high;
+  for (uint32_t t = 0; t < nt; t++) {
+    if (wires[t] >= n || (signs[t] & ~all)) return -1;
+    if (wires[t] >= 6 && std::find(high.begin(), high.end(), wires[t]) == high.end())
+      high.push_back(wires[t]);
+  }
+  if (high.size() > 4 || n < 6 + high.size()) return -1;
+  std::sort(high.begin(), high.end());
+  const uint32_t nh = static_cast<uint32_t>(high.size());
+  LocalAccumArgs c{};
+  c.nt = nt;
+  for (uint32_t j = 0; j < nh; j++) c.hpos[j] = high[j] - 6;
+  for (uint32_t t = 0; t < nt; t++) {
+    const uint32_t w = wires[t];
+    if (w == 0) {
+      c.kind[t] = 0;
+    } else if (w <= 5) {
+      c.kind[t] = 1;
+      c.arg[t] = static_cast<int8_t>(w - 1);
+    } else {
+      c.kind[t] = 2;
+      c.arg[t] = static_cast<int8_t>(std::find(high.begin(), high.end(), w) - high.begin());
+    }
+    c.sign[t] = signs[t];
+    for (uint32_t l = 0; l < (1u << nh); l++) {
+      uint64_t bits = 0;
+      for (uint32_t j = 0; j < nh; j++)
+        if ((l >> j) & 1) bits |= 1ull << high[j];      // amplitude bits of register l
+      c.lpar[t] |= static_cast<uint32_t>(__builtin_popcountll(bits & signs[t]) & 1) << l;
+    }
+    c.fpar |= static_cast<uint32_t>(__builtin_popcountll((1ull << w) & signs[t]) & 1) << t;
+    const double k = coeffs[t];
+    switch (ny[t] & 3u) {  // coeff * i^ny, exact
+      case 0: c.kappa[t] = make_float2(float(k), 0.f); break;
+      case 1: c.kappa[t] = make_float2(0.f, float(k)); break;
+      case 2: c.kappa[t] = make_float2(float(-k), 0.f); break;
+      default: c.kappa[t] = make_float2(0.f, float(-k)); break;
+    }
+  }
+  const uint64_t nw = 1ull << (n - 6 - nh);
+  const unsigned grid = grid_for(nw, kThreads / 32);
+  float4 *l4 = reinterpret_cast<float4 *>(lam);
+  const float4 *p4 = reinterpret_cast<const float4 *>(psi);
+  cudaStream_t s = (cudaStream_t)stream;
+  const bool ow = overwrite != 0;
+#define QMK_LOCAL_CASE(KH)                                                           \
+  if (nh == KH) {                                                                    \
+    if (ow) k_accum_local<KH, true><<<grid, kThreads, 0, s>>>(l4, p4, nw, c);        \
+    else k_accum_local<KH, false><<<grid, kThreads, 0, s>>>(l4, p4, nw, c);          \
+  }
+  QMK_LOCAL_CASE(0)
+  QMK_LOCAL_CASE(1)
+  QMK_LOCAL_CASE(2)
+  QMK_LOCAL_CASE(3)
+  QMK_LOCAL_CASE(4)
+#undef QMK_LOCAL_CASE
   return launch_status();
 }
 

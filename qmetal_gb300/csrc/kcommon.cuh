@@ -94,6 +94,12 @@ __device__ __forceinline__ uint64_t ins0(uint64_t x, uint32_t p) {
 
 __device__ __forceinline__ int parity64(uint64_t x) { return __popcll(x) & 1; }
 
+// The partner lane's vector (lane ^ mask), for ops on wires 1..5.
+__device__ __forceinline__ float4 shfl4(const float4 &v, int mask) {
+  return make_float4(__shfl_xor_sync(0xffffffffu, v.x, mask), __shfl_xor_sync(0xffffffffu, v.y, mask),
+                     __shfl_xor_sync(0xffffffffu, v.z, mask), __shfl_xor_sync(0xffffffffu, v.w, mask));
+}
+
 // e^{i phi} for an angle summed in FP64: reduced to [-pi, pi] in FP64, then
 // evaluated with the single-precision sincosf (about 1 ulp there).
 __device__ __forceinline__ float2 expi_reduced(double phi) {

@@ -557,15 +557,13 @@ void Simulator::run_merged(const Plan &p) {
     }
     for (uint32_t q : w)
       if (q >= n_) throw std::runtime_error("qubit index out of range");
-    std::vector<uint32_t> all = wires;
     bool overlap = false;
-    for (uint32_t q : w) {
+    for (uint32_t q : w)
       if (std::find(wires.begin(), wires.end(), q) != wires.end()) overlap = true;
-      all.push_back(q);
-    }
-    if (overlap || !fits(all)) flush();
-    // A group wider than one pass (never emitted by the default passes) goes
-    // wire by wire.
+    if (overlap) flush();
+    // The group's wires commute with each other and with the pending ones,
+    // so they join the pass one by one and spill into the next when it is
+    // full.
     for (size_t j = 0; j < w.size(); j++) {
       std::vector<uint32_t> trial = wires;
       trial.push_back(w[j]);
@@ -944,11 +942,101 @@ double Simulator::energy_and_costate(const Hamiltonian &h) {
                             zc.data(), d_results_, ws_, ws_bytes_, stream_),
           "co-state");
     dispatches_ += 2;
-  } else {
-    costate(h);
-    check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
-    dispatches_++;
+    return 0.0;
   }
+  // Mixed Hamiltonian: Z strings of <= 2 bits as one quadratic-form pass,
+  // terms that flip one wire many wires per pass, anything else one pass per
+  // flip mask; then the energy Re<psi|lambda>.
+  Hamiltonian zpart, local, rest;
+  for (const PauliTerm &t : h.terms) {
+    const uint64_t flip = t.pauli.x_mask | t.pauli.y_mask;
+    if (!flip && popc(t.pauli.z_mask) <= 2) zpart.terms.push_back(t);
+    else if (popc(flip) == 1 && n_ >= 6) local.terms.push_back(t);
+    else rest.terms.push_back(t);
+  }
+  bool first = true;
+  if (!zpart.terms.empty()) {
+    zm.clear();
+    zc.clear();
+    for (const PauliTerm &t : zpart.terms) {
+      zm.push_back(t.pauli.z_mask);
+      zc.push_back(t.coefficient);
+    }
+    check(qmk_zdiag_costate(costate_, state_, n_, static_cast<uint32_t>(zm.size()), zm.data(),
+                            zc.data(), d_results_, ws_, ws_bytes_, stream_),
+          "co-state");
+    dispatches_ += 2;
+    first = false;
+  }
+  if (!local.terms.empty()) {
+    // Tiles: wires 0..5 ride along in every pass; at most four wires >= 6
+    // and 16 terms per pass.
+    std::vector<size_t> order(local.terms.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = i;
+    auto wire_of = [&](size_t i) {
+      const PauliString &p = local.terms[i].pauli;
+      return static_cast<uint32_t>(__builtin_ctzll(p.x_mask | p.y_mask));
+    };
+    std::stable_sort(order.begin(), order.end(),
+                     [&](size_t a, size_t b) { return wire_of(a) < wire_of(b); });
+    const uint32_t max_high = std::min<uint32_t>(4, n_ - 6);
+    std::vector<uint32_t> wires, nys;
+    std::vector<uint64_t> signs;
+    std::vector<double> coeffs;
+    std::vector<uint32_t> highs;
+    auto flush = [&]() {
+      if (wires.empty()) return;
+      check(qmk_pauli_accum_local(costate_, state_, n_, static_cast<uint32_t>(wires.size()),
+                                  wires.data(), signs.data(), nys.data(), coeffs.data(),
+                                  first ? 1 : 0, stream_),
+            "co-state");
+      dispatches_++;
+      first = false;
+      wires.clear();
+      nys.clear();
+      signs.clear();
+      coeffs.clear();
+      highs.clear();
+    };
+    for (size_t i : order) {
+      const uint32_t w = wire_of(i);
+      const bool new_high =
+          w >= 6 && std::find(highs.begin(), highs.end(), w) == highs.end();
+      if (wires.size() == 16 || (new_high && highs.size() == max_high)) flush();
+      if (w >= 6 && std::find(highs.begin(), highs.end(), w) == highs.end()) highs.push_back(w);
+      const PauliString &p = local.terms[i].pauli;
+      wires.push_back(w);
+      signs.push_back(p.y_mask | p.z_mask);
+      nys.push_back(popc(p.y_mask));
+      coeffs.push_back(local.terms[i].coefficient);
+    }
+    flush();
+  }
+  if (!rest.terms.empty()) {
+    for (const FlipGroup &g : group_by_flip(rest)) {
+      for (size_t b = 0; b < g.terms.size(); b += kTermsPerPass) {
+        const uint32_t take =
+            static_cast<uint32_t>(std::min<size_t>(kTermsPerPass, g.terms.size() - b));
+        uint64_t signs[kTermsPerPass];
+        uint32_t nys[kTermsPerPass];
+        double coeffs[kTermsPerPass];
+        for (uint32_t j = 0; j < take; j++) {
+          const PauliTerm &t = rest.terms[g.terms[b + j]];
+          signs[j] = t.pauli.y_mask | t.pauli.z_mask;
+          nys[j] = popc(t.pauli.y_mask);
+          coeffs[j] = t.coefficient;
+        }
+        check(qmk_pauli_accum(costate_, state_, n_, g.flip, take, signs, nys, coeffs,
+                              first ? 1 : 0, stream_),
+              "co-state");
+        dispatches_++;
+        first = false;
+      }
+    }
+  }
+  if (first) cuda_check(cudaMemsetAsync(costate_, 0, dim() * 8, S(stream_)), "co-state zero");
+  check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
+  dispatches_++;
   return 0.0;
 }
 
@@ -1214,9 +1302,16 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
     reset();
     if (fused) run_merged(build_plan(c, FusionOptions{}));
     else run(build_plan(c, FusionOptions::none()));
-    energy_and_costate(h);
-    if (fused) sweep_fused(c);
-    else sweep_gate_by_gate(c);
+    if (fused) {
+      energy_and_costate(h);
+      sweep_fused(c);
+    } else {
+      // The reference's co-state: one pass per flip mask, then the energy.
+      costate(h);
+      check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
+      dispatches_++;
+      sweep_gate_by_gate(c);
+    }
     if (G)
       cuda_check(cudaMemcpyAsync(grad.data(), d_grad_, G * sizeof(double), cudaMemcpyDeviceToHost,
                                  S(stream_)),

@@ -107,3 +107,69 @@ def test_rejects_wire_sets_outside_every_route():
                                  flat.ctypes.data, None) != 0, wires
     qs = np.arange(11, dtype=np.uint32)
     assert L.qmk_apply_group(dev.data_ptr(), n, 11, qs.ctypes.data, flat.ctypes.data, None) != 0
+
+
+def _pauli_apply(state, n, flip, sign, ny, coeff):
+    """coeff * i^ny * P psi with P given by flip (x|y) and sign (y|z) masks:
+    (P psi)_i = (-1)^popcount((i ^ flip) & sign) psi_{i ^ flip}."""
+    idx = np.arange(1 << n)
+    src = idx ^ flip
+    par = np.array([bin(int(s) & sign).count("1") & 1 for s in src])
+    return coeff * (1j ** ny) * np.where(par, -1.0, 1.0) * state[src]
+
+
+@pytest.mark.parametrize("n", [6, 8, 12])
+def test_local_costate_terms(n):
+    """qmk_pauli_accum_local: many single-flip terms (X, Y with Z signs) in
+    one pass, overwrite and accumulate, against complex128."""
+    torch = pytest.importorskip("torch")
+    L = ctypes.CDLL(qm.library_path())
+    f = L.qmk_pauli_accum_local
+    f.restype = c_int
+    f.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_void_p,
+                  c_void_p, c_int, c_void_p]
+    rng = np.random.default_rng(300 + n)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    lam0 = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    high = sorted(rng.choice(np.arange(6, n), size=min(4, n - 6), replace=False).tolist()) \
+        if n > 6 else []
+    pool = list(range(6)) + high
+    for trial in range(6):
+        nt = int(rng.integers(1, 17))
+        wires = np.array([int(rng.choice(pool)) for _ in range(nt)], dtype=np.uint32)
+        ny = np.array([int(rng.integers(0, 2)) for _ in range(nt)], dtype=np.uint32)
+        signs = np.zeros(nt, dtype=np.uint64)
+        coeffs = rng.uniform(-1, 1, nt)
+        want = np.zeros(1 << n, dtype=complex)
+        for t in range(nt):
+            zmask = int(rng.integers(0, 1 << n)) & ~(1 << int(wires[t]))
+            ymask = (1 << int(wires[t])) if ny[t] else 0
+            signs[t] = ymask | zmask
+            want += _pauli_apply(psi, n, 1 << int(wires[t]), int(signs[t]), int(ny[t]),
+                                 coeffs[t])
+        overwrite = trial % 2
+        if not overwrite:
+            want += lam0
+        host_psi = np.empty(2 << n, dtype=np.float32)
+        host_psi[0::2], host_psi[1::2] = psi.real, psi.imag
+        host_lam = np.empty(2 << n, dtype=np.float32)
+        host_lam[0::2], host_lam[1::2] = lam0.real, lam0.imag
+        p = torch.from_numpy(host_psi).cuda()
+        lam = torch.from_numpy(host_lam).cuda()
+        assert f(lam.data_ptr(), p.data_ptr(), n, nt, wires.ctypes.data, signs.ctypes.data,
+                 ny.ctypes.data, coeffs.ctypes.data, overwrite, None) == 0
+        torch.cuda.synchronize()
+        out = lam.cpu().numpy()
+        got = out[0::2].astype(np.float64) + 1j * out[1::2]
+        assert np.abs(got - want).max() <= 1e-5, (n, trial)
+    # wires outside one tile, or too many terms, are refused before launch
+    if n >= 12:
+        wires = np.array([6, 7, 8, 9, 10], dtype=np.uint32)
+        z = np.zeros(5, dtype=np.uint64)
+        zi = np.zeros(5, dtype=np.uint32)
+        c1 = np.ones(5)
+        p = torch.zeros(2 << n, dtype=torch.float32, device="cuda")
+        lam = torch.zeros_like(p)
+        assert f(lam.data_ptr(), p.data_ptr(), n, 5, wires.ctypes.data, z.ctypes.data,
+                 zi.ctypes.data, c1.ctypes.data, 1, None) != 0
