@@ -39,6 +39,12 @@ sys.path.insert(0, ROOT)
 N_QUBITS = 30
 N_CPU = 20
 OP_NAMES = ["dense1q", "group", "blocked", "controlled1q", "diagonal", "swap", "ccx"]
+# DRAM bytes (read + write) per algorithmic byte of one launch, from the full
+# ncu captures at 26 qubits (profiles/group_diag_n26_full.md: k_group<4,0>
+# 536.9 + 475.8 MB, k_diag 537.0 + 477.4 MB against 2S = 1073.7 MB). The
+# traffic grows with the state, so a launch at n qubits moves this fraction
+# of its 2S.
+DRAM_PER_ALGO_BYTE = {1: (536.9 + 475.8) / 1073.7, 4: (537.0 + 477.4) / 1073.7}
 OP_STATE_PASSES = {0: 2.0, 1: 2.0, 2: 2.0, 3: 1.0, 4: 2.0, 5: 1.0, 6: 0.5}  # x S
 
 
@@ -248,6 +254,8 @@ def run_batch_workload(args, world, rank, dist):
     import qmetal_gb300 as qm
     from qmetal_gb300 import workloads as W
     insts = W.maxcut_instances(args.requests, seed=6)
+    if args.widths:
+        insts = [i for i in insts if i["n"] in args.widths]
     reqs = []
     for k, inst in enumerate(insts):
         gates = W.maxcut_qaoa(inst["n"], inst["edges"], inst["gammas"], inst["betas"])
@@ -272,13 +280,17 @@ def run_batch_workload(args, world, rank, dist):
             lanes_out, dt = serve(qm.BATCH_LANES)
             times.append(dt)
     wall = max_over_ranks(sum(times), dist, world)
-    plain_out, plain_t = serve(qm.BATCH_PLAIN_LOOP)
-    fused_out, fused_t = serve(qm.BATCH_FUSED_LOOP)
+    if args.no_loops:
+        plain_out, plain_t = lanes_out, float("nan")
+        fused_out, fused_t = lanes_out, float("nan")
+    else:
+        plain_out, plain_t = serve(qm.BATCH_PLAIN_LOOP)
+        fused_out, fused_t = serve(qm.BATCH_FUSED_LOOP)
     gdiff = max(float(np.max(np.abs(np.array(a[1]) - np.array(b[1])))) for a, b in
                 zip(lanes_out, plain_out))
     ediff = max(abs(a[0] - b[0]) for a, b in zip(lanes_out, plain_out))
     oracle_err = None
-    if rank == 0:
+    if rank == 0 and not args.no_loops:
         import oracle
         oracle.build()
         e_worst = g_worst = g_rel = 0.0
@@ -321,6 +333,10 @@ def run_batch_workload(args, world, rank, dist):
             "err_vs_complex128_oracle": oracle_err,
             "clocks": clocks.summary(),
         }
+        if args.no_loops:
+            for key in ("plain_loop", "blockwise_loop", "speedup_vs_plain_loop",
+                        "max_grad_diff_vs_plain", "max_energy_diff_vs_plain"):
+                line[key] = None
         print(json.dumps(line), flush=True)
     barrier(dist, world)
 
@@ -341,7 +357,9 @@ def run_grad_workload(args, world, rank, dist):
         nparams = sum(1 for g in gates if g[2])
         sim = qm.Simulator(n)
         entry = {"gates": len(gates), "params": nparams}
-        for label, fused in (("blockwise", True), ("gate_by_gate", False)):
+        modes = (("blockwise", True),) if args.no_loops else \
+            (("blockwise", True), ("gate_by_gate", False))
+        for label, fused in modes:
             sim.energy_and_gradient(c, h, fused=fused)      # warm-up
             sim.elapsed()
             reps = args.steps if fused else 1
@@ -352,9 +370,14 @@ def run_grad_workload(args, world, rank, dist):
                             "param_grads_per_s": round(nparams / t, 1)}
             entry.setdefault("energy", e)
             entry.setdefault("_grad", g)
+        g = entry.pop("_grad")
+        if args.no_loops:
+            results[f"n{n}"] = entry
+            sim.close()
+            del sim
+            continue
         entry["speedup"] = round(entry["gate_by_gate"]["s_per_gradient"]
                                  / entry["blockwise"]["s_per_gradient"], 2)
-        g = entry.pop("_grad")
         worst = 0.0
         eps = 1e-3
         for j in (0, len(gates) // 2, len(gates) - n - 2):
@@ -400,6 +423,11 @@ def main():
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--lanes", type=int, default=0,
                     help="batch lanes; 0 = autotuned on the batch's own requests")
+    ap.add_argument("--widths", type=int, nargs="+", default=None,
+                    help="batch: keep only the requests of these widths (profiling cases)")
+    ap.add_argument("--no-loops", action="store_true",
+                    help="batch / grad: time the block-wise path only (no per-circuit loops, "
+                         "no gate-by-gate sweep, no oracle or difference checks)")
     ap.add_argument("--cpu-qubits", type=int, default=N_CPU,
                     help="width of the bounded CPU sample (reference arm, cpu_baseline)")
     args = ap.parse_args()
@@ -553,7 +581,10 @@ def main():
             "roofline": {"bound": "hbm", "kernel": OP_NAMES[dom], "achieved": round(achieved, 1),
                          "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4),
                          "peak_source": peak_src,
-                         "traffic": None},
+                         "traffic": (round(DRAM_PER_ALGO_BYTE[dom] * op_bytes(dom, n))
+                                     if dom in DRAM_PER_ALGO_BYTE else None),
+                         "traffic_source": "ncu dram bytes per launch at n=26, scaled by "
+                                           "units to this n"},
             "kernels": breakdown,
             "frac_of_peak_overall": round(value / world / peak, 4),
             "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
