@@ -407,6 +407,116 @@ def run_grad_workload(args, world, rank, dist):
         print(json.dumps(line), flush=True)
 
 
+def benchmark_set(n, extended=False):
+    """The reference's frozen benchmark set at width n (src/circuits.cpp:
+    171-191): the five closed-form generators restated in workloads.py and
+    the mt19937-seeded members from the committed fixtures of the
+    reference's own generators (tests/golden/circuits.json)."""
+    from qmetal_gb300 import workloads as W
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "tests", "golden",
+                        "circuits.json")
+    with open(path) as f:
+        fixtures = json.load(f)
+
+    def fixture(key):
+        return [(k, tuple(q), tuple(p)) for k, q, p in fixtures[key]]
+
+    out = [("ghz", W.ghz(n)), ("qft", W.qft(n)), ("qaoa_ring_p6", W.qaoa_ring(n, 6)),
+           ("tfim_trotter_20", W.tfim_trotter(n, 20)), ("grover_proxy_4", W.grover_proxy(n, 4)),
+           ("random_d10", fixture(f"random_circuit_{n}_10_0x5eed")),
+           ("hea_d3", fixture(f"hardware_efficient_{n}_3_0x5eed"))]
+    if extended:
+        out.append(("local_patch_w8", fixture(f"local_patch_{n}_8_12_0x10ca1")))
+    return out
+
+
+def time_plan(sim, circuit, reps, **opts):
+    """Best device time of reps runs of one option set (reset excluded), as
+    the reference's benches take the best of their repetitions."""
+    best = float("inf")
+    for _ in range(reps + 1):
+        sim.reset()
+        sim.elapsed()
+        if opts.get("unfused"):
+            sim.run(circuit, fuse=False)
+        else:
+            sim.run_options(circuit, **{k: v for k, v in opts.items() if k != "unfused"})
+        best = min(best, sim.elapsed())
+    return best
+
+
+def run_fusion_workload(args, world, rank, dist):
+    """Port of the reference's fusion_bench (bench/fusion_bench.mm): the
+    frozen set at --ablation-qubits, unfused (one pass per gate) against the
+    default fused plan; speedup and pass ratio per circuit, geometric mean."""
+    import math
+    import qmetal_gb300 as qm
+    from qmetal_gb300 import workloads as W
+    n = args.ablation_qubits
+    sim = qm.Simulator(n)
+    rows, logsum = {}, 0.0
+    with ClockSampler(0) as clocks:
+        for name, gates in benchmark_set(n):
+            c = W.to_circuit(n, gates)
+            p0, p1 = c.plan_size(fuse=False), c.plan_size(fuse=True)
+            t0 = time_plan(sim, c, args.steps, unfused=True)
+            t1 = time_plan(sim, c, args.steps)
+            t0 = min(t0, time_plan(sim, c, args.steps, unfused=True))
+            t1 = min(t1, time_plan(sim, c, args.steps))
+            rows[name] = {"gates": len(gates), "passes_unfused": p0, "passes_fused": p1,
+                          "unfused_s": round(t0, 5), "fused_s": round(t1, 5),
+                          "speedup": round(t0 / t1, 2), "pass_ratio": round(p0 / p1, 2)}
+            logsum += math.log(t0 / t1)
+    if rank == 0:
+        print(json.dumps({
+            "metric": "fusion_speedup_geomean", "value": round(math.exp(logsum / len(rows)), 3),
+            "unit": "x", "n_gpus": world, "steps": args.steps, "higher_is_better": True,
+            "dtype": "c64", "data": "synthetic",
+            "config": {"workload": f"reference frozen benchmark set at n={n}, unfused vs fused "
+                                   "plan, best of steps", "num_qubits": n},
+            "circuits": rows, "clocks": clocks.summary()}), flush=True)
+
+
+def run_ablation_workload(args, world, rank, dist):
+    """Port of the reference's ablation (bench/ablation.mm): four arms --
+    no fusion, fusion, blocking alone, fusion + blocking (2^bits amplitude
+    blocks) -- interleaved, on the extended set; F/base, B/base and FB/F per
+    circuit and their geometric means."""
+    import math
+    import qmetal_gb300 as qm
+    from qmetal_gb300 import workloads as W
+    n, bits = args.ablation_qubits, args.block_bits
+    none = dict(collapse=False, diagonals=False, zz=False, group=1, block_bits=0)
+    arms = {"base": none, "F": dict(), "B": dict(none, block_bits=bits),
+            "FB": dict(block_bits=bits)}
+    sim = qm.Simulator(n)
+    rows = {}
+    logs = {"F/base": 0.0, "B/base": 0.0, "FB/F": 0.0}
+    with ClockSampler(0) as clocks:
+        for name, gates in benchmark_set(n, extended=True):
+            c = W.to_circuit(n, gates)
+            sizes = {a: int(c.plan_export(**o)[0]) for a, o in arms.items()}
+            t = {a: time_plan(sim, c, args.steps, **o) for a, o in arms.items()}
+            for a, o in arms.items():      # second interleaved round, best of both
+                t[a] = min(t[a], time_plan(sim, c, args.steps, **o))
+            r = {"F/base": t["base"] / t["F"], "B/base": t["base"] / t["B"],
+                 "FB/F": t["F"] / t["FB"]}
+            for k in logs:
+                logs[k] += math.log(r[k])
+            rows[name] = {"plan_ops": sizes, "seconds": {a: round(v, 5) for a, v in t.items()},
+                          **{k: round(v, 2) for k, v in r.items()}}
+    if rank == 0:
+        geo = {k: round(math.exp(v / len(rows)), 3) for k, v in logs.items()}
+        print(json.dumps({
+            "metric": "blocking_on_top_of_fusion_geomean", "value": geo["FB/F"], "unit": "x",
+            "n_gpus": world, "steps": args.steps, "higher_is_better": True, "dtype": "c64",
+            "data": "synthetic",
+            "config": {"workload": f"reference extended benchmark set at n={n}, four arms, "
+                                   f"block 2^{bits} amplitudes", "num_qubits": n,
+                       "block_bits": bits},
+            "geomean": geo, "circuits": rows, "clocks": clocks.summary()}), flush=True)
+
+
 def main():
     global N_CPU
     ap = argparse.ArgumentParser()
@@ -418,7 +528,12 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-scale", action="store_true",
                     help="skip the GHZ / QFT runs at 33 and 34 qubits")
-    ap.add_argument("--workload", default="fused30", choices=["fused30", "batch", "grad"])
+    ap.add_argument("--workload", default="fused30",
+                    choices=["fused30", "batch", "grad", "fusion", "ablation"])
+    ap.add_argument("--ablation-qubits", type=int, default=26,
+                    help="width of the fusion / ablation bench ports")
+    ap.add_argument("--block-bits", type=int, default=10,
+                    help="ablation: cache-blocking window, log2 amplitudes")
     ap.add_argument("--grad-qubits", type=int, nargs="+", default=[28, 33])
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--lanes", type=int, default=0,
@@ -438,6 +553,12 @@ def main():
         return
     if args.workload == "grad" and args.impl != "reference":
         run_grad_workload(args, world, rank, dist)
+        return
+    if args.workload == "fusion" and args.impl != "reference":
+        run_fusion_workload(args, world, rank, dist)
+        return
+    if args.workload == "ablation" and args.impl != "reference":
+        run_ablation_workload(args, world, rank, dist)
         return
     if args.impl == "reference":
         run_reference(args, world, rank, dist)
@@ -520,6 +641,22 @@ def main():
     e2e_wall = max_over_ranks(time.perf_counter() - t0, dist, world)
     e2e_value = world * args.steps * step_bytes / e2e_wall / 1e9
 
+    # --- the executor's merged form of the same plans (qm_run_merged): wider
+    # one-qubit passes and CX / SWAP runs as one permutation pass. Outside the
+    # roofline line, which is charged on the reference plan op for op.
+    merged = {}
+    for name, c in circuits:
+        sim.reset()
+        sim.run_merged(c)              # warm (takes the scratch buffer once)
+        sim.reset()
+        sim.elapsed()
+        d0m = sim.dispatch_count
+        sim.run_merged(c)
+        tm = sim.elapsed()
+        merged[name] = {"s": round(tm, 5), "launches": sim.dispatch_count - d0m,
+                        "plan_ops": c.plan_size()}
+    merged_s = sum(v["s"] for v in merged.values()) / len(merged)
+
     # --- scale: GHZ and QFT at 33 and 34 qubits (64 / 128 GiB in place) -------
     scale = {}
     if not args.no_scale:
@@ -594,6 +731,9 @@ def main():
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
             "wall_s_timed": round(wall, 3),
+            "merged": {"s_per_circuit": round(merged_s, 5),
+                       "speedup_vs_plan": round(dev_max / args.steps / len(circuits) / merged_s, 3),
+                       "circuits": merged},
         }
         print(json.dumps(line), flush=True)
     barrier(dist, world)

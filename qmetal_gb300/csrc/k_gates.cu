@@ -308,6 +308,90 @@ k_blocked(float2 *__restrict__ st, uint32_t b, uint64_t nblocks, BlockedArgs g) 
   }
 }
 
+// A block of b <= 10 low wires as a warp tile: lane = vector bits 0..4
+// (wires 1..5), registers = wires 6..b-1, wire 0 inside each vector. The
+// block's gates run in order on registers and shuffles, with no barrier and
+// no shared-memory round trip per gate; every global access is a whole
+// 512-byte warp access.
+constexpr int kSeqOps = 64;
+struct SeqArgs {
+  uint32_t count;
+  int8_t kind[kSeqOps];   // 0: wire 0, 1: lane bit, 2: register bit
+  int8_t arg[kSeqOps];
+  int8_t cls[kSeqOps];    // kMat* structure of m
+  M2 m[kSeqOps];
+};
+
+template <int NV, int J, int CLS>
+__device__ __forceinline__ void seq_reg(float4 (&P)[NV], const M2 &m) {
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    if ((l >> J) & 1) continue;
+    const int h = l | (1 << J);
+    float2 pa = lo2(P[l]), pb = lo2(P[h]), qa = hi2(P[l]), qb = hi2(P[h]);
+    apply2c(CLS, m, pa, pb);
+    apply2c(CLS, m, qa, qb);
+    P[l] = pack4(pa, qa);
+    P[h] = pack4(pb, qb);
+  }
+}
+
+template <int KH, int CLS>
+__device__ __forceinline__ void seq_op(float4 (&P)[1 << KH], int kind, int arg, const M2 &m,
+                                       uint32_t lane) {
+  constexpr int NV = 1 << KH;
+  if (kind == 0) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      float2 p0 = lo2(P[l]), p1 = hi2(P[l]);
+      apply2c(CLS, m, p0, p1);
+      P[l] = pack4(p0, p1);
+    }
+  } else if (kind == 1) {
+    const bool one = (lane >> arg) & 1;
+    const float2 s = one ? m.d : m.a, t = one ? m.c : m.b;
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      const float4 o = (CLS == kMatDiag) ? P[l] : shfl4(P[l], 1 << arg);
+      P[l] = pack4(cmac2c(CLS, s, lo2(P[l]), t, lo2(o)), cmac2c(CLS, s, hi2(P[l]), t, hi2(o)));
+    }
+  } else {
+    if (KH > 0 && arg == 0) seq_reg<NV, 0, CLS>(P, m);
+    if (KH > 1 && arg == 1) seq_reg<NV, (KH > 1 ? 1 : 0), CLS>(P, m);
+    if (KH > 2 && arg == 2) seq_reg<NV, (KH > 2 ? 2 : 0), CLS>(P, m);
+    if (KH > 3 && arg == 3) seq_reg<NV, (KH > 3 ? 3 : 0), CLS>(P, m);
+  }
+}
+
+template <int KH>
+__global__ void __launch_bounds__(kThreads)
+k_seq_warp(float4 *__restrict__ st, uint64_t nwsites, SeqArgs g) {
+  constexpr int NV = 1 << KH;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
+  for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
+    // registers take vector bits 5 .. 4 + KH (wires 6 .. 5 + KH); the site
+    // index fills the bits above them
+    const uint64_t base = (ws << (5 + KH)) | lane;
+    float4 P[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) P[l] = st[base | (static_cast<uint64_t>(l) << 5)];
+    for (uint32_t o = 0; o < g.count; o++) {
+      const int kind = g.kind[o], arg = g.arg[o];
+      const M2 m = g.m[o];
+      switch (g.cls[o]) {
+        case kMatReal: seq_op<KH, kMatReal>(P, kind, arg, m, lane); break;
+        case kMatRx: seq_op<KH, kMatRx>(P, kind, arg, m, lane); break;
+        case kMatDiag: seq_op<KH, kMatDiag>(P, kind, arg, m, lane); break;
+        default: seq_op<KH, kMatGeneral>(P, kind, arg, m, lane); break;
+      }
+    }
+#pragma unroll
+    for (int l = 0; l < NV; l++) st[base | (static_cast<uint64_t>(l) << 5)] = P[l];
+  }
+}
+
 // Swap for wires a < b. A0: a == 0, so lane z,w of vector v (a=1,b=0) trades
 // with lanes x,y of v|tb (a=0,b=1). Otherwise whole vectors trade.
 template <bool A0>
@@ -541,6 +625,35 @@ extern "C" int qmk_apply_blocked(float *state, uint32_t n, uint32_t b,
   if (count && (!qubits || !mats)) return -1;
   for (uint32_t k = 0; k < count; k++)
     if (qubits[k] >= b) return -1;
+  const uint32_t tile = b < 6 ? 6u : b;           // wires the warp tile spans
+  if (b <= 10 && n >= tile) {
+    const int kh = static_cast<int>(tile) - 6;
+    const uint64_t nw = 1ull << (n - 1 - 5 - kh);
+    const unsigned grid = grid_for(nw, kThreads / 32);
+    float4 *st = reinterpret_cast<float4 *>(state);
+    cudaStream_t s = (cudaStream_t)stream;
+    uint32_t done = 0;
+    do {
+      SeqArgs g{};
+      g.count = std::min<uint32_t>(count - done, kSeqOps);
+      for (uint32_t k = 0; k < g.count; k++) {
+        const uint32_t q = qubits[done + k];
+        g.kind[k] = q == 0 ? 0 : (q <= 5 ? 1 : 2);
+        g.arg[k] = static_cast<int8_t>(q == 0 ? 0 : (q <= 5 ? q - 1 : q - 6));
+        g.m[k] = m2_from(mats + 8 * (done + k));
+        g.cls[k] = m2_class(g.m[k]);
+      }
+      switch (kh) {
+        case 0: k_seq_warp<0><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+        case 1: k_seq_warp<1><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+        case 2: k_seq_warp<2><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+        case 3: k_seq_warp<3><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+        default: k_seq_warp<4><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+      }
+      done += g.count;
+    } while (done < count);
+    return launch_status();
+  }
   const size_t smem = sizeof(float2) << b;
   if (smem > 48 * 1024) {
     cudaError_t e = cudaFuncSetAttribute(k_blocked, cudaFuncAttributeMaxDynamicSharedMemorySize,

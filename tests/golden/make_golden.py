@@ -38,6 +38,7 @@ SEEDED = [
     ("random_circuit", 5, 4, 0xABC),
 ]
 FROZEN_N = [4, 6, 7, 10, 11, 14, 20]
+BENCH_N = [26]           # the width of the reference's fusion and ablation benches
 
 
 def frozen(n):
@@ -60,9 +61,13 @@ def main():
     circuits = {}
     for name, n, d, seed in SEEDED:
         circuits[f"{name}_{n}_{d}_{seed:#x}"] = oracle.ref_circuit(name, n, d, 0, seed)
-    for n in FROZEN_N:
+    for n in FROZEN_N + BENCH_N:
         circuits[f"random_circuit_{n}_10_0x5eed"] = oracle.ref_circuit("random_circuit", n, 10, 0, 0x5EED)
         circuits[f"hardware_efficient_{n}_3_0x5eed"] = oracle.ref_circuit("hardware_efficient", n, 3, 0, 0x5EED)
+    # The ablation set's extra member, local_patch(n, 8, 12) with its default
+    # seed (src/circuits.cpp:133-168, include/qmetal/circuits.h:57-58).
+    for n in (14,) + tuple(BENCH_N):
+        circuits[f"local_patch_{n}_8_12_0x10ca1"] = oracle.ref_circuit("local_patch", n, 8, 12, 0x10CA1)
     with open(os.path.join(HERE, "circuits.json"), "w") as f:
         json.dump({k: [[g[0], list(g[1]), list(g[2])] for g in v] for k, v in circuits.items()}, f)
 

@@ -148,8 +148,10 @@ def test_register_groups_with_wires_inside_a_warp(k):
             assert np.abs(sim.get_state() - want).max() <= 1e-5, (n, wires)
 
 
-@pytest.mark.parametrize("bits", [2, 5, 8, 12])
+@pytest.mark.parametrize("bits", [2, 5, 6, 8, 9, 10, 11, 12])
 def test_blocked_kernel(bits, golden_circuits):
+    """Blocks of b <= 10 wires run as a warp tile, wider ones in shared
+    memory; long runs with repeated wires, every matrix form."""
     n = 13
     gates = golden_circuits["hardware_efficient_14_3_0x5eed"]
     gates = [(k, qs, ps) for k, qs, ps in gates if max(qs) < n]
@@ -157,6 +159,22 @@ def test_blocked_kernel(bits, golden_circuits):
     sim = qm.Simulator(n)
     sim.run_options(W.to_circuit(n, local), block_bits=bits)
     assert np.abs(sim.get_state() - oracle.run(n, local)).max() <= 1e-5
+    # blocking without fusion: long uncollapsed runs (more gates than one
+    # launch takes), every one-qubit kind, on a random state
+    rng = np.random.default_rng(bits)
+    init = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    init /= np.linalg.norm(init)
+    run = []
+    for k in range(150):
+        q = int(rng.integers(0, bits))
+        kind = int(rng.choice([X, Y, Z, H, S, SDG, T, TDG, RX, RY, RZ, P]))
+        run.append((kind, (q,), (float(rng.uniform(-3, 3)),) if kind >= RX else ()))
+    run += [(CX, (0, n - 1), ())] + run[:30]
+    sim = qm.Simulator(n)
+    sim.set_state(init)
+    sim.run_options(W.to_circuit(n, run), collapse=False, diagonals=False, zz=False, group=1,
+                    block_bits=bits)
+    assert np.abs(sim.get_state() - oracle.run(n, run, init)).max() <= 1e-5
 
 
 @pytest.mark.parametrize("n", [6, 10, 14, 20])
