@@ -49,15 +49,39 @@ struct OutSlots {
   __device__ void operator()(int t, double s) const { p[slot[t]] = s; }
 };
 
+constexpr int pow2_at_least(int t) { return t <= 1 ? 1 : 2 * pow2_at_least((t + 1) / 2); }
+
 template <int T, typename Out>
 __device__ __forceinline__ void finish(double (&acc)[T], int nt, Area a, const Out &out) {
+  static_assert(T >= 1 && T <= 32, "at most 32 results per reduction");
   __shared__ double red[kThreads / 32][T > 0 ? T : 1];
   __shared__ unsigned ticket;
   const int w = threadIdx.x >> 5, l = threadIdx.x & 31;
+  if constexpr (T == 1) {
+    const double v = warp_sum(acc[0]);
+    if (l == 0) red[w][0] = v;
+  } else {
+    // Transposed butterfly: each step halves the slots a lane carries and
+    // trades the other half with its partner, so lane l ends with slot l
+    // summed over the warp: P - 1 exchanges for P slots instead of 5 P
+    // (FP64 adds run at a small fraction of the FP32 rate on this part).
+    constexpr int P = pow2_at_least(T);
+    double v[P];
 #pragma unroll
-  for (int t = 0; t < T; t++) {
-    const double v = warp_sum(acc[t]);
-    if (l == 0) red[w][t] = v;
+    for (int t = 0; t < P; t++) v[t] = t < T ? acc[t] : 0.0;
+#pragma unroll
+    for (int h = P / 2; h >= 1; h >>= 1) {
+      const bool upper = (l & h) != 0;
+#pragma unroll
+      for (int j = 0; j < h; j++) {
+        const double send = upper ? v[j] : v[j + h];
+        const double keep = upper ? v[j + h] : v[j];
+        v[j] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+      }
+    }
+#pragma unroll
+    for (int o = P; o < 32; o <<= 1) v[0] += __shfl_xor_sync(0xffffffffu, v[0], o);
+    if (l < T) red[w][l] = v[0];
   }
   __syncthreads();
   if (threadIdx.x < static_cast<unsigned>(nt)) {
