@@ -344,40 +344,88 @@ __device__ __forceinline__ float re_dot4(const float4 &l, const float4 &w) {
 // wire's 0 side and (d, c) on its 1 side, and it takes its own half of the
 // pair's overlap: X: Im(conj(l) other); Y: -/+ Re(conj(l) other); Z: +/-
 // Im(conj(l) own). A diagonal op needs no partner unless its generator is X
-// or Y (a rotation by zero).
-template <int NV, int CLS>
-__device__ __forceinline__ float lane_op(float4 (&P)[NV], float4 (&L)[NV], int mask, bool one,
-                                         int gen, const M2 &m) {
+// or Y (a rotation by zero). GEN is a template parameter so the unrolled
+// body has no branch and the vectors' chains interleave.
+template <int NV, int CLS, int GEN>
+__device__ __forceinline__ float lane_op_g(float4 (&P)[NV], float4 (&L)[NV], int mask, bool one,
+                                           const M2 &m) {
   const float2 s = one ? m.d : m.a, t = one ? m.c : m.b;
-  float ov = 0.0f;
+  float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
 #pragma unroll
   for (int l = 0; l < NV; l++) {
-    if (CLS == kMatDiag && gen != 1 && gen != 2) {
-      if (gen == 3) ov += im_dot4(L[l], P[l]);
+    if (CLS == kMatDiag && GEN != 1 && GEN != 2) {
+      if (GEN == 3) acc[l & 3] += im_dot4(L[l], P[l]);
       P[l] = pack4(cmac2c(CLS, s, lo2(P[l]), t, lo2(P[l])), cmac2c(CLS, s, hi2(P[l]), t, hi2(P[l])));
       L[l] = pack4(cmac2c(CLS, s, lo2(L[l]), t, lo2(L[l])), cmac2c(CLS, s, hi2(L[l]), t, hi2(L[l])));
     } else {
       const float4 Po = shfl4(P[l], mask), Lo = shfl4(L[l], mask);
-      if (gen == 1) ov += im_dot4(L[l], Po);
-      else if (gen == 2) ov += re_dot4(L[l], Po);
-      else if (gen == 3) ov += im_dot4(L[l], P[l]);
+      if (GEN == 1) acc[l & 3] += im_dot4(L[l], Po);
+      if (GEN == 2) acc[l & 3] += re_dot4(L[l], Po);
+      if (GEN == 3) acc[l & 3] += im_dot4(L[l], P[l]);
       P[l] = pack4(cmac2c(CLS, s, lo2(P[l]), t, lo2(Po)), cmac2c(CLS, s, hi2(P[l]), t, hi2(Po)));
       L[l] = pack4(cmac2c(CLS, s, lo2(L[l]), t, lo2(Lo)), cmac2c(CLS, s, hi2(L[l]), t, hi2(Lo)));
     }
   }
-  if (gen == 2) return one ? ov : -ov;
-  if (gen == 3) return one ? -ov : ov;
+  const float ov = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  if (GEN == 2) return one ? ov : -ov;
+  if (GEN == 3) return one ? -ov : ov;
   return ov;
+}
+
+template <int NV, int CLS>
+__device__ __forceinline__ float lane_op(float4 (&P)[NV], float4 (&L)[NV], int mask, bool one,
+                                         int gen, const M2 &m) {
+  switch (gen) {
+    case 1: return lane_op_g<NV, CLS, 1>(P, L, mask, one, m);
+    case 2: return lane_op_g<NV, CLS, 2>(P, L, mask, one, m);
+    case 3: return lane_op_g<NV, CLS, 3>(P, L, mask, one, m);
+    default: return lane_op_g<NV, CLS, 0>(P, L, mask, one, m);
+  }
+}
+
+// Overlap of the pairs (p0, p1) = (P[l], P[h]) or the two halves of one
+// vector, before the op is applied: a separate loop per generator, so the
+// apply loop that follows is branch free.
+template <int GEN>
+__device__ __forceinline__ float pair_ov(const float4 &pa, const float4 &pb, const float4 &la,
+                                         const float4 &lb) {
+  return overlap(GEN, lo2(pa), lo2(pb), lo2(la), lo2(lb)) +
+         overlap(GEN, hi2(pa), hi2(pb), hi2(la), hi2(lb));
+}
+
+template <int NV, int GEN>
+__device__ __forceinline__ float wire0_ov(const float4 (&P)[NV], const float4 (&L)[NV]) {
+  float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int l = 0; l < NV; l++)
+    acc[l & 3] += overlap(GEN, lo2(P[l]), hi2(P[l]), lo2(L[l]), hi2(L[l]));
+  return (acc[0] + acc[1]) + (acc[2] + acc[3]);
+}
+
+template <int NV, int J, int GEN>
+__device__ __forceinline__ float reg_ov(const float4 (&P)[NV], const float4 (&L)[NV]) {
+  float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  int k = 0;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    if ((l >> J) & 1) continue;
+    const int h = l | (1 << J);
+    acc[k & 3] += pair_ov<GEN>(P[l], P[h], L[l], L[h]);
+    k++;
+  }
+  return (acc[0] + acc[1]) + (acc[2] + acc[3]);
 }
 
 // One op on wire 0 (the two amplitudes of each vector).
 template <int NV, int CLS>
 __device__ __forceinline__ float wire0_op(float4 (&P)[NV], float4 (&L)[NV], int gen, const M2 &m) {
   float ov = 0.0f;
+  if (gen == 1) ov = wire0_ov<NV, 1>(P, L);
+  else if (gen == 2) ov = wire0_ov<NV, 2>(P, L);
+  else if (gen == 3) ov = wire0_ov<NV, 3>(P, L);
 #pragma unroll
   for (int l = 0; l < NV; l++) {
     float2 p0 = lo2(P[l]), p1 = hi2(P[l]), l0 = lo2(L[l]), l1 = hi2(L[l]);
-    if (gen) ov += overlap(gen, p0, p1, l0, l1);
     apply2c(CLS, m, p0, p1);
     apply2c(CLS, m, l0, l1);
     P[l] = pack4(p0, p1);
@@ -390,13 +438,15 @@ __device__ __forceinline__ float wire0_op(float4 (&P)[NV], float4 (&L)[NV], int 
 template <int NV, int J, int CLS>
 __device__ __forceinline__ float reg_op(float4 (&P)[NV], float4 (&L)[NV], int gen, const M2 &m) {
   float ov = 0.0f;
+  if (gen == 1) ov = reg_ov<NV, J, 1>(P, L);
+  else if (gen == 2) ov = reg_ov<NV, J, 2>(P, L);
+  else if (gen == 3) ov = reg_ov<NV, J, 3>(P, L);
 #pragma unroll
   for (int l = 0; l < NV; l++) {
     if ((l >> J) & 1) continue;
     const int h = l | (1 << J);
     float2 pa = lo2(P[l]), pb = lo2(P[h]), qa = hi2(P[l]), qb = hi2(P[h]);
     float2 la = lo2(L[l]), lb = lo2(L[h]), ma = hi2(L[l]), mb = hi2(L[h]);
-    if (gen) ov += overlap(gen, pa, pb, la, lb) + overlap(gen, qa, qb, ma, mb);
     apply2c(CLS, m, pa, pb);
     apply2c(CLS, m, qa, qb);
     apply2c(CLS, m, la, lb);
@@ -429,8 +479,9 @@ __device__ __forceinline__ float warp_op(float4 (&P)[NV], float4 (&L)[NV], int k
   return reg_op_any<NV, CLS>(P, L, arg, gen, m);
 }
 
+// Tiles of up to three register wires keep two blocks resident per SM.
 template <int KH, int NG>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, KH >= 4 ? 1 : 2)
 k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, WarpAdjArgs g,
            Area a, OutSlots<(NG > 0 ? NG : 1)> out) {
   constexpr int NV = 1 << KH;

@@ -49,7 +49,9 @@ struct OutSlots {
   __device__ void operator()(int t, double s) const { p[slot[t]] = s; }
 };
 
-constexpr int pow2_at_least(int t) { return t <= 1 ? 1 : 2 * pow2_at_least((t + 1) / 2); }
+__host__ __device__ constexpr int pow2_at_least(int t) {
+  return t <= 1 ? 1 : 2 * pow2_at_least((t + 1) / 2);
+}
 
 template <int T, typename Out>
 __device__ __forceinline__ void finish(double (&acc)[T], int nt, Area a, const Out &out) {
