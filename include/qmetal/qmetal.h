@@ -190,11 +190,20 @@ typedef struct {
  *         block-wise adjoint, one synchronisation per request;
  * mode 1: one request after another as a per-circuit caller would run them
  *         (gate-by-gate adjoint, then run and sample);
- * mode 2: one request after another with the block-wise adjoint.
- * Every mode returns the same numbers to within float round-off. In mode 0,
- * lanes = 0 uses the autotuned lane count and tile shapes (tuning first if
- * this set of widths has not been tuned in this process). */
+ * mode 2: one request after another with the block-wise adjoint;
+ * mode 3: every request recorded into one CUDA graph (branches per width,
+ *         heavy widths split up to four ways) and launched once, results staged in
+ *         pinned memory by copy nodes; one synchronisation for the batch.
+ * Every mode returns the same numbers to within float round-off. In modes 0
+ * and 3, lanes = 0 uses the autotuned tile shapes (and in mode 0 lane count),
+ * tuning first if this set of widths has not been tuned in this process. */
 int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t lanes);
+
+/* Where the calling thread's last mode-3 batch spent its time: recording
+ * (host work of every request while the graph records), instantiation, and
+ * the single launch to completion; and the graph's node count. */
+int qm_batch_graph_timing(double *out_record_s, double *out_instantiate_s,
+                          double *out_execute_s, uint64_t *out_nodes);
 
 /* Tune a batch on its own requests (their outputs are overwritten): per
  * width, the number of wires >= 6 each backward window pass holds in

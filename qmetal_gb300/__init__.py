@@ -135,6 +135,8 @@ class _BatchItem(ctypes.Structure):
 
 
 _batch_serve = _decl("qm_batch_serve", c_int, POINTER(_BatchItem), c_size_t, c_int, c_uint32)
+_batch_graph_timing = _decl("qm_batch_graph_timing", c_int, POINTER(c_double), POINTER(c_double),
+                            POINTER(c_double), POINTER(c_uint64))
 _batch_autotune = _decl("qm_batch_autotune", c_int, POINTER(_BatchItem), c_size_t, _u32p, _u32p,
                         _f64p)
 _run_profiled = _decl("qm_run_profiled", c_int, c_void_p, c_void_p, c_int, _f64p,
@@ -445,7 +447,16 @@ class Simulator:
         return out.value
 
 
-BATCH_LANES, BATCH_PLAIN_LOOP, BATCH_FUSED_LOOP = 0, 1, 2
+BATCH_LANES, BATCH_PLAIN_LOOP, BATCH_FUSED_LOOP, BATCH_GRAPH = 0, 1, 2, 3
+
+
+def batch_graph_timing():
+    """Seconds the calling thread's last BATCH_GRAPH batch spent recording,
+    instantiating and executing its graph, and the graph's node count."""
+    r, i, e, nodes = c_double(), c_double(), c_double(), c_uint64()
+    _check(_batch_graph_timing(byref(r), byref(i), byref(e), byref(nodes)))
+    return {"record_s": r.value, "instantiate_s": i.value, "execute_s": e.value,
+            "nodes": int(nodes.value)}
 
 
 def _batch_items(requests):

@@ -19,6 +19,8 @@
 #include <algorithm>
 #include <atomic>
 #include <chrono>
+#include <cmath>
+#include <cstring>
 #include <map>
 #include <memory>
 #include <mutex>
@@ -102,6 +104,140 @@ void serve_lanes(const std::vector<BatchItem> &items, const std::vector<size_t> 
   if (failed.load()) throw std::runtime_error("batch: " + first_error);
 }
 
+thread_local GraphTiming g_graph_timing;
+
+double seconds_since(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+}
+
+// Every request recorded into one CUDA graph and launched once. Requests of a
+// width share a simulator (its requests follow each other in the graph); the
+// widths are parallel branches forked from and joined into one origin stream,
+// and a heavy width is split over up to four simulators, about one per eighth
+// of the batch's state traffic. Results land in pinned staging memory through
+// copy nodes and are handed out after the single synchronisation.
+void serve_graph(const std::vector<BatchItem> &items, const std::vector<size_t> &order,
+                 const BatchTuning *tuning) {
+  GraphTiming timing;
+  const auto t_record = std::chrono::steady_clock::now();
+  // Branches: per width, split in two when it carries > 1/4 of the traffic.
+  std::map<uint32_t, std::vector<size_t>> by_width;
+  double total = 0.0;
+  std::map<uint32_t, double> weight;
+  for (size_t i : order) {
+    const uint32_t n = items[i].circuit->num_qubits;
+    by_width[n].push_back(i);
+    const double w = std::ldexp(1.0, static_cast<int>(n)) * (1.0 + items[i].circuit->ops.size());
+    weight[n] += w;
+    total += w;
+  }
+  std::vector<std::vector<size_t>> branches;
+  std::vector<uint32_t> branch_width;
+  for (auto it = by_width.rbegin(); it != by_width.rend(); ++it) {
+    // about one branch per eighth of the traffic, at most four per width
+    const int share = static_cast<int>(std::lround(8.0 * weight[it->first] / total));
+    const int parts = static_cast<int>(std::min<size_t>(
+        it->second.size(), static_cast<size_t>(std::max(1, std::min(4, share)))));
+    for (int p = 0; p < parts; p++) {
+      branches.emplace_back();
+      branch_width.push_back(it->first);
+      for (size_t k = p; k < it->second.size(); k += parts) branches.back().push_back(it->second[k]);
+    }
+  }
+  // Simulators and buffers first: nothing allocates while the graph records.
+  std::vector<std::unique_ptr<Simulator>> sims;
+  size_t staging = 0;
+  std::vector<size_t> offset(items.size());
+  for (size_t b = 0; b < branches.size(); b++) {
+    size_t max_gates = 1, max_shots = 0;
+    for (size_t i : branches[b]) {
+      max_gates = std::max(max_gates, items[i].circuit->ops.size());
+      max_shots = std::max(max_shots, items[i].shots);
+      offset[i] = staging;
+      staging += 1 + items[i].circuit->ops.size() + items[i].shots;
+    }
+    sims.emplace_back(new Simulator(branch_width[b]));
+    if (tuning) sims.back()->set_tile_high(tuning->tile_high[branch_width[b]]);
+    sims.back()->reserve(max_gates, max_shots);
+  }
+  uint64_t *pinned = nullptr;
+  if (cudaMallocHost(&pinned, std::max<size_t>(staging, 1) * sizeof(uint64_t)) != cudaSuccess)
+    throw std::runtime_error("batch: pinned staging allocation failed");
+  cudaStream_t origin = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  std::vector<cudaEvent_t> events;
+  auto cleanup = [&]() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : events) cudaEventDestroy(e);
+    if (origin) cudaStreamDestroy(origin);
+    cudaFreeHost(pinned);
+  };
+  try {
+    if (cudaStreamCreateWithFlags(&origin, cudaStreamNonBlocking) != cudaSuccess)
+      throw std::runtime_error("batch: stream creation failed");
+    for (size_t k = 0; k < branches.size() + 1; k++) {
+      cudaEvent_t e;
+      if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess)
+        throw std::runtime_error("batch: event creation failed");
+      events.push_back(e);
+    }
+    for (auto &s : sims) s->synchronize();
+    if (cudaStreamBeginCapture(origin, cudaStreamCaptureModeRelaxed) != cudaSuccess)
+      throw std::runtime_error("batch: graph capture failed to start");
+    try {
+      cudaEventRecord(events[0], origin);
+      for (size_t b = 0; b < branches.size(); b++) {
+        cudaStream_t s = static_cast<cudaStream_t>(sims[b]->stream());
+        cudaStreamWaitEvent(s, events[0], 0);
+        for (size_t i : branches[b]) {
+          const BatchItem &it = items[i];
+          uint64_t *slot = pinned + offset[i];
+          sims[b]->serve_enqueue(*it.circuit, *it.hamiltonian, it.shots, it.seed,
+                                 reinterpret_cast<double *>(slot),
+                                 reinterpret_cast<double *>(slot + 1), slot + 1 +
+                                     it.circuit->ops.size());
+        }
+        cudaEventRecord(events[b + 1], s);
+        cudaStreamWaitEvent(origin, events[b + 1], 0);
+      }
+    } catch (...) {
+      cudaStreamEndCapture(origin, &graph);
+      throw;
+    }
+    if (cudaStreamEndCapture(origin, &graph) != cudaSuccess || !graph)
+      throw std::runtime_error("batch: graph capture failed");
+    timing.record_s = seconds_since(t_record);
+    cudaGraphGetNodes(graph, nullptr, &timing.nodes);
+    timing.branches = branches.size();
+    const auto t_inst = std::chrono::steady_clock::now();
+    if (cudaGraphInstantiate(&exec, graph, 0) != cudaSuccess)
+      throw std::runtime_error("batch: graph instantiation failed");
+    timing.instantiate_s = seconds_since(t_inst);
+    const auto t_exec = std::chrono::steady_clock::now();
+    if (cudaGraphLaunch(exec, origin) != cudaSuccess)
+      throw std::runtime_error("batch: graph launch failed");
+    const cudaError_t e = cudaStreamSynchronize(origin);
+    if (e != cudaSuccess) throw std::runtime_error(std::string("batch: ") + cudaGetErrorString(e));
+    timing.execute_s = seconds_since(t_exec);
+    for (const BatchItem &it : items) {
+      const uint64_t *slot = pinned + offset[&it - items.data()];
+      if (it.energy) std::memcpy(it.energy, slot, sizeof(double));
+      if (!it.circuit->ops.empty())
+        std::memcpy(it.grad, slot + 1, it.circuit->ops.size() * sizeof(double));
+      if (it.shots)
+        std::memcpy(it.samples, slot + 1 + it.circuit->ops.size(), it.shots * sizeof(uint64_t));
+    }
+  } catch (...) {
+    cudaStreamSynchronize(origin);
+    cleanup();
+    throw;
+  }
+  cleanup();
+  g_graph_timing = timing;
+}
+
 std::mutex g_tuning_lock;
 std::map<std::vector<uint32_t>, BatchTuning> g_tuning_cache;
 
@@ -175,7 +311,7 @@ void run_batch(const std::vector<BatchItem> &items, BatchMode mode, uint32_t lan
   if (cudaGetDevice(&device) != cudaSuccess) throw std::runtime_error("batch: no CUDA device");
   const std::vector<size_t> order = widest_first(items);
 
-  if (mode != BatchMode::Lanes) {
+  if (mode == BatchMode::PlainLoop || mode == BatchMode::FusedLoop) {
     std::map<uint32_t, std::unique_ptr<Simulator>> sims;
     for (size_t idx : order) {
       const BatchItem &it = items[idx];
@@ -188,6 +324,15 @@ void run_batch(const std::vector<BatchItem> &items, BatchMode mode, uint32_t lan
     }
     return;
   }
+  if (mode == BatchMode::Graph) {
+    if (lanes == 0) {
+      const BatchTuning tuned = autotune_batch(items);
+      serve_graph(items, order, &tuned);
+    } else {
+      serve_graph(items, order, nullptr);
+    }
+    return;
+  }
   if (lanes == 0) {
     const BatchTuning tuned = autotune_batch(items);
     serve_lanes(items, order, tuned.lanes, &tuned, device);
@@ -195,5 +340,7 @@ void run_batch(const std::vector<BatchItem> &items, BatchMode mode, uint32_t lan
   }
   serve_lanes(items, order, lanes, nullptr, device);
 }
+
+GraphTiming last_graph_timing() { return g_graph_timing; }
 
 }  // namespace qmetal

@@ -23,7 +23,18 @@ enum class BatchMode {
   Lanes = 0,       // concurrent lanes, block-wise adjoint, one sync per request
   PlainLoop = 1,   // one request after another, gate-by-gate adjoint, then run + sample
   FusedLoop = 2,   // one request after another, block-wise adjoint
+  Graph = 3,       // every request recorded into one CUDA graph, launched once
 };
+
+// Time split of the last Graph-mode batch served by this thread.
+struct GraphTiming {
+  double record_s = 0.0;        // host: building and recording every request
+  double instantiate_s = 0.0;   // cudaGraphInstantiate
+  double execute_s = 0.0;       // one launch to completion
+  size_t nodes = 0;
+  size_t branches = 0;
+};
+GraphTiming last_graph_timing();
 
 // Choices the autotuner makes for a batch: how many lanes run at once, and per
 // width the tile shape of the backward window passes (wires >= 6 held in

@@ -423,8 +423,8 @@ int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t 
     set_error("null argument");
     return -1;
   }
-  if (mode < 0 || mode > 2) {
-    set_error("batch mode must be 0, 1 or 2");
+  if (mode < 0 || mode > 3) {
+    set_error("batch mode must be 0, 1, 2 or 3");
     return -1;
   }
   return guarded([&] {
@@ -444,6 +444,16 @@ int qm_batch_serve(const qm_batch_item *items, size_t count, int mode, uint32_t 
     }
     run_batch(v, static_cast<BatchMode>(mode), lanes);
   });
+}
+
+int qm_batch_graph_timing(double *out_record_s, double *out_instantiate_s,
+                          double *out_execute_s, uint64_t *out_nodes) {
+  const GraphTiming t = last_graph_timing();
+  if (out_record_s) *out_record_s = t.record_s;
+  if (out_instantiate_s) *out_instantiate_s = t.instantiate_s;
+  if (out_execute_s) *out_execute_s = t.execute_s;
+  if (out_nodes) *out_nodes = t.nodes;
+  return 0;
 }
 
 int qm_batch_autotune(const qm_batch_item *items, size_t count, uint32_t *out_lanes,

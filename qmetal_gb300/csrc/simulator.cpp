@@ -1351,6 +1351,62 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
   if (energy) *energy = h_results_[0];
 }
 
+void Simulator::reserve(size_t max_gates, size_t max_shots) {
+  activate();
+  if (!costate_) {
+    size_t free_b = 0, total_b = 0;
+    cuda_check(cudaMemGetInfo(&free_b, &total_b), "cudaMemGetInfo");
+    if (dim() * 8 > free_b) throw std::runtime_error("gradient: co-state does not fit on the device");
+    cuda_check(cudaMalloc(&costate_, dim() * 8), "gradient: co-state allocation failed");
+  }
+  const size_t G = std::max<size_t>(max_gates, 1);
+  if (d_grad_cap_ < G) {
+    cudaFree(d_grad_);
+    d_grad_ = nullptr;
+    d_grad_cap_ = 0;
+    cuda_check(cudaMalloc(&d_grad_, G * sizeof(double)), "gradient buffer");
+    d_grad_cap_ = G;
+  }
+  if (!sample_ws_) {
+    sample_ws_bytes_ = qmk_sample_workspace_bytes(n_);
+    cuda_check(cudaMalloc(&sample_ws_, sample_ws_bytes_), "sampling workspace");
+  }
+  if (max_shots && d_shots_cap_ < max_shots) {
+    cudaFree(d_shots_);
+    d_shots_ = nullptr;
+    d_shots_cap_ = 0;
+    cuda_check(cudaMalloc(&d_shots_, max_shots * sizeof(uint64_t)), "sampling output");
+    d_shots_cap_ = max_shots;
+  }
+  ensure_scratch();
+}
+
+void Simulator::serve_enqueue(const Circuit &c, const Hamiltonian &h, size_t shots, uint64_t seed,
+                              double *pinned_energy, double *pinned_grad,
+                              uint64_t *pinned_samples) {
+  if (d_grad_cap_ < std::max<size_t>(c.ops.size(), 1) || !costate_ ||
+      (shots && (d_shots_cap_ < shots || !sample_ws_)))
+    throw std::runtime_error("serve_enqueue: buffers not reserved for this request");
+  prepare_adjoint(c, h);
+  reset();
+  run_merged(build_plan(c, FusionOptions{}));
+  if (shots) launch_sample(shots, seed);
+  energy_and_costate(h);
+  sweep_fused(c);
+  if (!c.ops.empty() && pinned_grad)
+    cuda_check(cudaMemcpyAsync(pinned_grad, d_grad_, c.ops.size() * sizeof(double),
+                               cudaMemcpyDeviceToHost, S(stream_)),
+               "gradient copy");
+  if (shots && pinned_samples)
+    cuda_check(cudaMemcpyAsync(pinned_samples, d_shots_, shots * sizeof(uint64_t),
+                               cudaMemcpyDeviceToHost, S(stream_)),
+               "sample copy");
+  if (pinned_energy)
+    cuda_check(cudaMemcpyAsync(pinned_energy, d_results_, sizeof(double), cudaMemcpyDeviceToHost,
+                               S(stream_)),
+               "energy copy");
+}
+
 double Simulator::elapsed() {
   activate();
   cudaEvent_t a = static_cast<cudaEvent_t>(ev_start_), b = static_cast<cudaEvent_t>(ev_stop_);

@@ -70,6 +70,15 @@ class Simulator {
   // one queued sequence with a single synchronisation.
   void serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint64_t seed, double *energy,
              double *grad, uint64_t *samples);
+  // The same sequence queued only, with its results copied into pinned host
+  // memory by the stream (energy: one double, grad: one per gate, samples:
+  // shots). After reserve() it allocates and synchronises nothing, so it can
+  // be recorded into a CUDA graph.
+  void serve_enqueue(const Circuit &c, const Hamiltonian &h, size_t shots, uint64_t seed,
+                     double *pinned_energy, double *pinned_grad, uint64_t *pinned_samples);
+  // Device buffers for requests of up to max_gates gates and max_shots shots.
+  void reserve(size_t max_gates, size_t max_shots);
+  void *stream() const { return stream_; }
 
   // Tile shape of the block-wise sweep's window passes: how many wires >= 6
   // one two-state pass holds in registers (1..4, besides wire 0 and the five

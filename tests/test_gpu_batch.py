@@ -147,3 +147,23 @@ def test_autotuned_lanes_and_tile_shapes():
         assert abs(e - e0) <= ETOL
         assert np.abs(np.array(g) - g0).max() <= GTOL
         assert s == b[2]      # the forward state, hence the draws, is unchanged
+
+
+def test_graph_mode_matches_the_loop():
+    """BATCH_GRAPH records every request into one CUDA graph (branches per
+    width, heavy widths split up to four ways) and launches it once: the kernel
+    sequence per request is the block-wise loop's, so the results are the
+    same bits; the oracle bounds them too."""
+    reqs = requests(20, seed=31, n_lo=8, n_hi=16, shots=256)
+    graph = run_mode(reqs, qm.BATCH_GRAPH, lanes=1)
+    timing = qm.batch_graph_timing()
+    assert timing["nodes"] > len(reqs) and timing["execute_s"] > 0
+    fused = run_mode(reqs, qm.BATCH_FUSED_LOOP)
+    for (inst, gates, terms, _s, _seed), a, b in zip(reqs, graph, fused):
+        assert a[0] == b[0] and a[1] == b[1] and a[2] == b[2]
+        e0, g0 = oracle.energy_and_gradient(inst["n"], gates, terms)
+        assert abs(a[0] - e0) <= ETOL
+        assert np.abs(np.array(a[1]) - g0).max() <= GTOL
+    # a second batch reuses nothing from the first and still agrees
+    again = run_mode(reqs, qm.BATCH_GRAPH, lanes=1)
+    assert [x[0] for x in again] == [x[0] for x in graph]
