@@ -501,3 +501,47 @@ def test_u3_every_wire(mode):
     # U3 carries parameters without a native generator: the gradient fails closed
     with pytest.raises(qm.QMetalError, match="differentiable"):
         sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian([(1.0, 0, 0, 1)]))
+
+
+@pytest.mark.parametrize("n", [1, 2, 3, 4, 5, 6, 7])
+def test_gradients_on_the_smallest_states(n):
+    """Widths below and at the edges of the tile shapes (fewer wires than a
+    warp's lanes, one register wire): every sweep path, mixed Hamiltonians
+    with X, Y and Z strings, CX ladders and SWAPs, against the oracle."""
+    rng = np.random.default_rng(700 + n)
+    gates = [(H, (q,), ()) for q in range(n)]
+    for layer in range(3):
+        for q in range(n):
+            gates.append(((RX, RY, RZ)[(q + layer) % 3], (q,), (float(rng.uniform(-3, 3)),)))
+        if n >= 2:
+            gates += [(CX, (q, q + 1), ()) for q in range(n - 1)]
+            gates.append((SWAP, (0, n - 1), ()))
+            a, b = int(rng.integers(n)), int(rng.integers(n))
+            if a != b:
+                gates += [(CX, (a, b), ()), (RZ, (b,), (float(rng.uniform(-2, 2)),)),
+                          (CX, (a, b), ())]
+    terms = [(0.7, 1 << q, 0, 0) for q in range(n)] + [(-0.4, 0, 1 << (n - 1), 0)]
+    terms += [(0.5, 0, 0, (1 << q) | (1 << ((q + 1) % n))) for q in range(n)]
+    if n >= 3:
+        terms.append((0.3, 1, 1 << 1, 1 << 2))          # X0 Y1 Z2
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    c, h = W.to_circuit(n, gates), W.to_hamiltonian(terms)
+    for fused in (True, False):
+        e, g = qm.Simulator(n).energy_and_gradient(c, h, fused=fused)
+        assert abs(e - e0) <= 1e-5, fused
+        assert np.abs(np.array(g) - g0).max() <= 1e-5, fused
+    # and through the batch paths, widths 1..n mixed
+    reqs = []
+    for m in range(1, n + 1):
+        gm = [(RY, (q,), (0.3 + 0.1 * q,)) for q in range(m)]
+        gm += [(CX, (q, q + 1), ()) for q in range(m - 1)] + [(RX, (0,), (0.9,))]
+        reqs.append((W.to_circuit(m, gm), W.to_hamiltonian([(1.0, 0, 0, 1), (0.5, 1, 0, 0)]),
+                     32, m))
+    for mode in (qm.BATCH_LANES, qm.BATCH_GRAPH, qm.BATCH_PLAIN_LOOP):
+        out = qm.batch_serve(reqs, mode=mode, lanes=2)
+        for m, (e, g, s) in zip(range(1, n + 1), out):
+            gm = [(RY, (q,), (0.3 + 0.1 * q,)) for q in range(m)]
+            gm += [(CX, (q, q + 1), ()) for q in range(m - 1)] + [(RX, (0,), (0.9,))]
+            e1, g1 = oracle.energy_and_gradient(m, gm, [(1.0, 0, 0, 1), (0.5, 1, 0, 0)])
+            assert abs(e - e1) <= 1e-5 and np.abs(np.array(g) - g1).max() <= 1e-5, (mode, m)
+            assert len(s) == 32 and all(0 <= x < (1 << m) for x in s)
