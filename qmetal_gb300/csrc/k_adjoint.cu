@@ -322,7 +322,8 @@ constexpr int kMaxWarpOps = 32;
 struct WarpAdjArgs {
   uint32_t nops, ngrad;
   uint32_t hpos[4];              // wires >= 6: vector bit - 5, ascending
-  int8_t kind[kMaxWarpOps];      // 0: wire 0, 1: lane bit, 2: register bit
+  int8_t kind[kMaxWarpOps];      // 0: wire 0, 1: lane bit, 2: register bit,
+                                 // 3: the wire split across a warp pair
   int8_t arg[kMaxWarpOps];       // lane bit (0..4) or register index
   int8_t gen[kMaxWarpOps];
   int8_t slotidx[kMaxWarpOps];
@@ -542,6 +543,180 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Window tiles with four wires >= 6, two warps per tile: each thread holds the
+// eight vectors of both states for three of the four register wires, and the
+// two warps of a pair hold the two values of the fourth. An op on that fourth
+// wire trades the pair's vectors through shared memory (each thread then
+// takes its own half, as a lane op does); every other op is the one-warp
+// tile's. Half the registers per thread of the one-warp tile, so twice the
+// resident warps to hide the loads and the dependent arithmetic.
+
+constexpr int kPairNV = 8;
+
+// The op on the fourth wire for every register vector: own' = s own + t
+// other, own half of the overlap; the partner's vectors come from shared
+// memory (written before the barrier that precedes this call).
+template <int CLS, int GEN>
+__device__ __forceinline__ float split_op_g(float4 (&P)[kPairNV], float4 (&L)[kPairNV],
+                                            const float4 *__restrict__ oth_p,
+                                            const float4 *__restrict__ oth_l, bool one,
+                                            const M2 &m) {
+  const float2 s = one ? m.d : m.a, t = one ? m.c : m.b;
+  float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int l = 0; l < kPairNV; l++) {
+    const float4 Po = oth_p[l * 32], Lo = oth_l[l * 32];
+    if (GEN == 1) acc[l & 3] += im_dot4(L[l], Po);
+    if (GEN == 2) acc[l & 3] += re_dot4(L[l], Po);
+    if (GEN == 3) acc[l & 3] += im_dot4(L[l], P[l]);
+    P[l] = pack4(cmac2c(CLS, s, lo2(P[l]), t, lo2(Po)), cmac2c(CLS, s, hi2(P[l]), t, hi2(Po)));
+    L[l] = pack4(cmac2c(CLS, s, lo2(L[l]), t, lo2(Lo)), cmac2c(CLS, s, hi2(L[l]), t, hi2(Lo)));
+  }
+  const float ov = (acc[0] + acc[1]) + (acc[2] + acc[3]);
+  if (GEN == 2) return one ? ov : -ov;
+  if (GEN == 3) return one ? -ov : ov;
+  return ov;
+}
+
+template <int CLS>
+__device__ __forceinline__ float split_op(float4 (&P)[kPairNV], float4 (&L)[kPairNV],
+                                          const float4 *oth_p, const float4 *oth_l, bool one,
+                                          int gen, const M2 &m) {
+  switch (gen) {
+    case 1: return split_op_g<CLS, 1>(P, L, oth_p, oth_l, one, m);
+    case 2: return split_op_g<CLS, 2>(P, L, oth_p, oth_l, one, m);
+    case 3: return split_op_g<CLS, 3>(P, L, oth_p, oth_l, one, m);
+    default: return split_op_g<CLS, 0>(P, L, oth_p, oth_l, one, m);
+  }
+}
+
+template <int NG>
+__global__ void __launch_bounds__(kThreads, 2)
+k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, WarpAdjArgs g,
+           Area a, OutSlots<(NG > 0 ? NG : 1)> out) {
+  constexpr int NV = kPairNV;
+  constexpr int NA = NG > 0 ? NG : 1;
+  extern __shared__ __align__(16) float4 xs[];   // [warp][state][NV][32 lanes]
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t half = warp & 1;                // value of the fourth wire
+  const uint64_t per_round = static_cast<uint64_t>(gridDim.x) * (kThreads / 64);
+  const uint64_t rounds = (nwsites + per_round - 1) / per_round;
+  float4 *mine_p = xs + (warp * 2 + 0) * NV * 32 + lane;
+  float4 *mine_l = xs + (warp * 2 + 1) * NV * 32 + lane;
+  const float4 *oth_p = xs + ((warp ^ 1) * 2 + 0) * NV * 32 + lane;
+  const float4 *oth_l = xs + ((warp ^ 1) * 2 + 1) * NV * 32 + lane;
+  float accf[NA];
+#pragma unroll
+  for (int t = 0; t < NA; t++) accf[t] = 0.0f;
+  // Every warp of the block runs the same number of rounds (the barriers of
+  // the exchanges must match); a pair past the last tile works on zeros and
+  // stores nothing.
+  for (uint64_t r = 0; r < rounds; r++) {
+    const uint64_t ws = r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) +
+                        (warp >> 1);
+    const bool active = ws < nwsites;
+    uint64_t base = 0;
+    if (active) {
+      uint64_t b = ws;
+#pragma unroll
+      for (int j = 0; j < 4; j++) b = ins0(b, g.hpos[j]);
+      base = (b << 5) | lane | (static_cast<uint64_t>(half) << (g.hpos[3] + 5));
+    }
+    auto vec_of = [&](int l) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      return v;
+    };
+    float4 P[NV], L[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      if (active) {
+        const uint64_t v = vec_of(l);
+        P[l] = psi[v];
+        L[l] = lam[v];
+      } else {
+        P[l] = L[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    for (uint32_t o = 0; o < g.nops; o++) {
+      const int kind = g.kind[o], arg = g.arg[o], gen = g.gen[o], cls = g.cls[o];
+      const M2 m = g.m[o];
+      float ov;
+      if (kind == 3) {
+        const bool need = cls != kMatDiag || gen == 1 || gen == 2;
+        if (need) {
+#pragma unroll
+          for (int l = 0; l < NV; l++) {
+            mine_p[l * 32] = P[l];
+            mine_l[l * 32] = L[l];
+          }
+          __syncthreads();
+        }
+        const bool one = half != 0;
+        switch (cls) {
+          case kMatReal: ov = split_op<kMatReal>(P, L, oth_p, oth_l, one, gen, m); break;
+          case kMatRx: ov = split_op<kMatRx>(P, L, oth_p, oth_l, one, gen, m); break;
+          case kMatDiag: ov = split_op<kMatDiag>(P, L, oth_p, oth_l, one, gen, m); break;
+          default: ov = split_op<kMatGeneral>(P, L, oth_p, oth_l, one, gen, m); break;
+        }
+        if (need) __syncthreads();
+      } else {
+        switch (cls) {
+          case kMatReal: ov = warp_op<NV, kMatReal>(P, L, kind, arg, gen, m, lane); break;
+          case kMatRx: ov = warp_op<NV, kMatRx>(P, L, kind, arg, gen, m, lane); break;
+          case kMatDiag: ov = warp_op<NV, kMatDiag>(P, L, kind, arg, gen, m, lane); break;
+          default: ov = warp_op<NV, kMatGeneral>(P, L, kind, arg, gen, m, lane); break;
+        }
+      }
+      if (NG > 0 && gen) {
+#pragma unroll
+        for (int t = 0; t < NA; t++)
+          if (t == g.slotidx[o]) accf[t] += ov;
+      }
+    }
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        const uint64_t v = vec_of(l);
+        psi[v] = P[l];
+        lam[v] = L[l];
+      }
+    }
+  }
+  if constexpr (NG > 0) {
+    double acc[NA];
+#pragma unroll
+    for (int t = 0; t < NA; t++) acc[t] = accf[t];
+    finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
+  }
+}
+
+template <int NG>
+int launch_adj_pair(float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArgs &g,
+                    const OutSlots<kMaxGen> &slots, Area a, cudaStream_t s) {
+  OutSlots<(NG > 0 ? NG : 1)> out{};
+  out.p = slots.p;
+  for (int t = 0; t < (NG > 0 ? NG : 1); t++) out.slot[t] = slots.slot[t];
+  unsigned grid = grid_for(nwsites, kThreads / 64);
+  grid = std::min<unsigned>(grid, reduce_grid());
+  const size_t smem = static_cast<size_t>(kThreads / 32) * 2 * kPairNV * 32 * sizeof(float4);
+  // The opt-in above 48 KiB is per device; set it once on each.
+  static bool opted[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (!opted[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_adj_pair<NG>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    opted[dev] = true;
+  }
+  k_adj_pair<NG><<<grid, kThreads, smem, s>>>(psi, lam, nwsites, g, a, out);
+  return launch_status();
+}
+
 template <int KH, int NG>
 void launch_adj_warp(float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArgs &g,
                      const OutSlots<kMaxGen> &slots, Area a, cudaStream_t s) {
@@ -745,6 +920,15 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
     cudaStream_t s = (cudaStream_t)stream;
     const Area a = area_of(ws);
     const int ng = ngrad == 0 ? 0 : (ngrad <= 4 ? 4 : (ngrad <= 8 ? 8 : 16));
+    if (nh == 4) {
+      // two warps per tile: the fourth register wire is split across the pair
+      for (uint32_t o = 0; o < nops; o++)
+        if (g.kind[o] == 2 && g.arg[o] == 3) g.kind[o] = 3;
+      if (ng == 0) return launch_adj_pair<0>(p4, l4, nw, g, out, a, s);
+      if (ng == 4) return launch_adj_pair<4>(p4, l4, nw, g, out, a, s);
+      if (ng == 8) return launch_adj_pair<8>(p4, l4, nw, g, out, a, s);
+      return launch_adj_pair<16>(p4, l4, nw, g, out, a, s);
+    }
 #define QMK_ADJ_WARP_CASE(KH)                                                   \
     if (nh == KH) {                                                             \
       if (ng == 0) launch_adj_warp<KH, 0>(p4, l4, nw, g, out, a, s);            \
