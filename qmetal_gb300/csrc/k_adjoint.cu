@@ -114,23 +114,29 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
   float accf[T > 0 ? T : 1];
 #pragma unroll
   for (int t = 0; t < (T > 0 ? T : 1); t++) accf[t] = 0.0f;
+  // Generator signs outside the 32 transformed amplitudes: bit t is the
+  // parity of (fixed bits & fixmask[t]); the thread's own bits give a mask
+  // that holds for every tile, the tile's bits one that every thread shares
+  // (lane t computes bit t, a ballot hands the word to the warp).
+  __shared__ uint64_t fm[T > 0 ? T : 1];
+  uint32_t own_sign = 0;
+  if (T > 0) {
+    const uint64_t mine = static_cast<uint64_t>(tid) << 1;
+    for (int t = 0; t < T && t < static_cast<int>(g.ngen); t++)
+      own_sign |= static_cast<uint32_t>(parity64(mine & g.fixmask[t])) << t;
+    if (tid < static_cast<uint32_t>(T)) fm[tid] = g.fixmask[tid];
+  }
+  __syncthreads();
+  const uint32_t lane = tid & 31;
   for (uint64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-    if (g.undo) {
-      tile_coeffs<true>(d, tile, f, &eH, nullptr, nullptr, true);
-      __syncthreads();
-      tile_phase_tables(W, f, eH, Y1, Y2);
-      __syncthreads();
-    }
     const uint64_t base = tile << (W - 1);
-    float F[32];
-#pragma unroll
-    for (int j = 0; j < 32; j++) F[j] = 0.0f;
     // Four vectors of both states (and their table entries) are loaded
-    // before any is used, so each thread keeps 8-12 loads in flight.
+    // before any is used, so each thread keeps 8-12 loads in flight; the
+    // first four are issued before the tile's phase tables are built, so the
+    // table set-up runs under their latency.
     constexpr int UU = 4;
-#pragma unroll
-    for (int c = 0; c < 16; c += UU) {
-      float4 P[UU], L[UU], tb[UU];
+    float4 P[UU], L[UU], tb[UU];
+    auto load_chunk = [&](int c) {
 #pragma unroll
       for (int u = 0; u < UU; u++) {
         const uint32_t e = tid + (c + u) * kThreads;
@@ -140,6 +146,20 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
           if (g.undo) tb[u] = table4[e];
         }
       }
+    };
+    load_chunk(0);
+    if (g.undo) {
+      tile_coeffs<true>(d, tile, f, &eH, nullptr, nullptr, true);
+      __syncthreads();
+      tile_phase_tables(W, f, eH, Y1, Y2);
+      __syncthreads();
+    }
+    float F[32];
+#pragma unroll
+    for (int j = 0; j < 32; j++) F[j] = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 16; c += UU) {
+      if (c > 0) load_chunk(c);
 #pragma unroll
       for (int u = 0; u < UU; u++) {
         const int k = c + u;
@@ -178,12 +198,16 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
       float *row = &Fs[tid * 33];
 #pragma unroll
       for (int j = 0; j < 32; j++) row[j] = F[j];
-      const uint64_t fixed = (tile << W) | (static_cast<uint64_t>(tid) << 1);
       const int ng = static_cast<int>(g.ngen);
+      const uint64_t tbits = tile << W;
+      const bool mine = static_cast<int>(lane) < ng && static_cast<int>(lane) < T;
+      const uint32_t tile_sign =
+          __ballot_sync(0xffffffffu, mine && parity64(tbits & fm[lane < T ? lane : 0]));
+      const uint32_t sign = own_sign ^ tile_sign;
 #pragma unroll
       for (int t = 0; t < T; t++) {
         const float v = t < ng ? row[g.vm[t]] : 0.0f;
-        accf[t] += parity64(fixed & g.fixmask[t]) ? -v : v;
+        accf[t] += ((sign >> t) & 1u) ? -v : v;
       }
     }
     __syncthreads();
