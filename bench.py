@@ -443,7 +443,11 @@ def benchmark_set(n, extended=False):
            ("random_d10", fixture(f"random_circuit_{n}_10_0x5eed")),
            ("hea_d3", fixture(f"hardware_efficient_{n}_3_0x5eed"))]
     if extended:
-        out.append(("local_patch_w8", fixture(f"local_patch_{n}_8_12_0x10ca1")))
+        patch = fixture(f"local_patch_{n}_8_12_0x10ca1")
+        out.append(("local_patch_w8", patch))
+        # the same work register on the highest wires, where blocking cannot
+        # reach it unless the qubits are reordered
+        out.append(("local_patch_w8_high", W.relabel(patch, [n - 1 - q for q in range(n)])))
     return out
 
 
@@ -498,7 +502,11 @@ def run_ablation_workload(args, world, rank, dist):
     """Port of the reference's ablation (bench/ablation.mm): four arms --
     no fusion, fusion, blocking alone, fusion + blocking (2^bits amplitude
     blocks) -- interleaved, on the extended set; F/base, B/base and FB/F per
-    circuit and their geometric means."""
+    circuit and their geometric means. A fifth arm, FBR, tests the qubit
+    reordering the reference left untested (results/S4_RESULT.md): the
+    wires with the most one-qubit gates are relabeled into the block window,
+    the relabeled circuit runs fused and blocked, and one permutation pass
+    restores the qubit order (timed)."""
     import math
     import qmetal_gb300 as qm
     from qmetal_gb300 import workloads as W
@@ -508,16 +516,35 @@ def run_ablation_workload(args, world, rank, dist):
             "FB": dict(block_bits=bits)}
     sim = qm.Simulator(n)
     rows = {}
-    logs = {"F/base": 0.0, "B/base": 0.0, "FB/F": 0.0}
+    logs = {"F/base": 0.0, "B/base": 0.0, "FB/F": 0.0, "FBR/F": 0.0}
     with ClockSampler(0) as clocks:
         for name, gates in benchmark_set(n, extended=True):
             c = W.to_circuit(n, gates)
             sizes = {a: int(c.plan_export(**o)[0]) for a, o in arms.items()}
+            perm = W.hot_wires_first(n, gates)
+            back = [0] * n
+            for q, p in enumerate(perm):
+                back[p] = q
+            cr = W.to_circuit(n, W.relabel(gates, perm))
+            sizes["FBR"] = int(cr.plan_export(block_bits=bits)[0]) + 1
+
+            def remap_arm():
+                best = float("inf")
+                for _ in range(args.steps + 1):
+                    sim.reset()
+                    sim.elapsed()
+                    sim.run_options(cr, block_bits=bits)
+                    sim.permute_qubits(back)
+                    best = min(best, sim.elapsed())
+                return best
+
             t = {a: time_plan(sim, c, args.steps, **o) for a, o in arms.items()}
+            t["FBR"] = remap_arm()
             for a, o in arms.items():      # second interleaved round, best of both
                 t[a] = min(t[a], time_plan(sim, c, args.steps, **o))
+            t["FBR"] = min(t["FBR"], remap_arm())
             r = {"F/base": t["base"] / t["F"], "B/base": t["base"] / t["B"],
-                 "FB/F": t["F"] / t["FB"]}
+                 "FB/F": t["F"] / t["FB"], "FBR/F": t["F"] / t["FBR"]}
             for k in logs:
                 logs[k] += math.log(r[k])
             rows[name] = {"plan_ops": sizes, "seconds": {a: round(v, 5) for a, v in t.items()},

@@ -137,6 +137,14 @@ int qm_run_cached(qm_simulator s, qm_circuit c);
  * qm_run; the reference has no counterpart. */
 int qm_run_merged(qm_simulator s, qm_circuit c);
 
+/* Relabel the state's qubits: afterwards qubit perm[q] holds what qubit q
+ * held (perm is a permutation of 0..n-1). One out-of-place pass through the
+ * GF(2) permutation kernel; the second state buffer is taken on first use. A
+ * circuit relabeled the same way then runs on the relabeled state, so a
+ * caller can move frequently used qubits into a cache-blocking window (the
+ * reference's untested "qubit reordering", results/S4_RESULT.md). */
+int qm_permute_qubits(qm_simulator s, const uint32_t *perm, uint32_t count);
+
 /* Run with explicit fusion options (FusionOptions, reference plan.h:76-94). */
 int qm_run_options(qm_simulator s, qm_circuit c, int collapse_1q_windows,
                    int fuse_diagonals, int recognize_zz, uint32_t group_1q,

@@ -103,6 +103,7 @@ _run = _decl("qm_run", c_int, c_void_p, c_void_p)
 _run_unfused = _decl("qm_run_unfused", c_int, c_void_p, c_void_p)
 _run_cached = _decl("qm_run_cached", c_int, c_void_p, c_void_p)
 _run_merged = _decl("qm_run_merged", c_int, c_void_p, c_void_p)
+_permute_qubits = _decl("qm_permute_qubits", c_int, c_void_p, _u32p, c_uint32)
 _run_options = _decl("qm_run_options", c_int, c_void_p, c_void_p, c_int, c_int,
                      c_int, c_uint32, c_uint32)
 _sync = _decl("qm_synchronize", c_int, c_void_p)
@@ -325,6 +326,13 @@ class Simulator:
         """run() with the executor's merging on top of the plan: wider
         one-qubit passes and CX / SWAP runs as one permutation pass."""
         _check(_run_merged(self._h, circuit._h))
+        return self
+
+    def permute_qubits(self, perm):
+        """Relabel the state's qubits: qubit perm[q] then holds what qubit q
+        held (one permutation pass)."""
+        arr = (c_uint32 * len(perm))(*[int(p) for p in perm])
+        _check(_permute_qubits(self._h, arr, len(perm)))
         return self
 
     def run_cached(self, circuit: Circuit):

@@ -233,6 +233,14 @@ int qm_run_merged(qm_simulator s, qm_circuit c) {
   return guarded([&] { s->s->run_merged(c->c); });
 }
 
+int qm_permute_qubits(qm_simulator s, const uint32_t *perm, uint32_t count) {
+  if (!s || (count && !perm)) {
+    set_error("null argument");
+    return -1;
+  }
+  return guarded([&] { s->s->permute_qubits(std::vector<uint32_t>(perm, perm + count)); });
+}
+
 int qm_run_unfused(qm_simulator s, qm_circuit c) {
   if (!s || !c) {
     set_error("null argument");

@@ -576,6 +576,25 @@ void Simulator::run_merged(const Plan &p) {
   flush_run();
 }
 
+void Simulator::permute_qubits(const std::vector<uint32_t> &perm) {
+  if (perm.size() != n_) throw std::runtime_error("permute_qubits: one target per qubit");
+  std::vector<bool> seen(n_, false);
+  for (uint32_t p : perm) {
+    if (p >= n_ || seen[p]) throw std::runtime_error("permute_qubits: not a permutation");
+    seen[p] = true;
+  }
+  activate();
+  // new[x'] = old[x] with bit perm[q] of x' = bit q of x, i.e. a gather with
+  // G(x') = sum over set bits perm[q] of x' of e_q.
+  std::vector<uint64_t> cols(n_);
+  for (uint32_t q = 0; q < n_; q++) cols[perm[q]] = 1ull << q;
+  bool identity = true;
+  for (uint32_t q = 0; q < n_; q++) identity &= perm[q] == q;
+  if (identity) return;
+  if (!permute(state_, cols, 0))
+    throw std::runtime_error("permute_qubits: no room for the second state buffer");
+}
+
 void Simulator::run_merged(const Circuit &c) {
   if (c.num_qubits != n_) throw std::runtime_error("circuit/simulator size mismatch");
   run_merged(build_plan(c, FusionOptions{}));

@@ -40,6 +40,9 @@ class Simulator {
   // permutation pass where that moves fewer bytes (same unitary, fewer passes).
   void run_merged(const Plan &p);
   void run_merged(const Circuit &c);
+  // Relabel the qubits of the state: afterwards wire perm[q] holds what wire
+  // q held (one out-of-place permutation pass).
+  void permute_qubits(const std::vector<uint32_t> &perm);
   // Runs the plan with a CUDA event between ops; seconds[i] = op i's device time.
   void run_profiled(const Plan &p, std::vector<double> &seconds);
   void synchronize();

@@ -32,6 +32,25 @@ def to_circuit(n, gates):
     return c
 
 
+def hot_wires_first(n, gates):
+    """Qubit relabeling that puts the wires with the most one-qubit gates on
+    the lowest indices (ties keep their order): perm[q] is q's new index."""
+    count = [0] * n
+    for _k, qs, _ps in gates:
+        if len(qs) == 1:
+            count[qs[0]] += 1
+    order = sorted(range(n), key=lambda q: -count[q])
+    perm = [0] * n
+    for new, q in enumerate(order):
+        perm[q] = new
+    return perm
+
+
+def relabel(gates, perm):
+    """The gate stream with every qubit q renamed perm[q]."""
+    return [(k, tuple(perm[q] for q in qs), ps) for k, qs, ps in gates]
+
+
 def _zz(out, a, b, theta):
     # exp(-i theta Z_a Z_b) as CX / RZ(2 theta) / CX (src/circuits.cpp:11-16)
     out += [(CX, (a, b), ()), (RZ, (b,), (2.0 * theta,)), (CX, (a, b), ())]

@@ -32,7 +32,7 @@ def test_frozen_set_gate_counts_match_reference_bench():
     got = {name: len(g) for name, g in _bench().benchmark_set(26)}
     assert got == want
     ext = dict(_bench().benchmark_set(26, extended=True))
-    assert set(ext) == set(want) | {"local_patch_w8"}
+    assert set(ext) == set(want) | {"local_patch_w8", "local_patch_w8_high"}
 
 
 @pytest.mark.parametrize("opts", [dict(), dict(collapse=False, diagonals=False, zz=False,
@@ -44,3 +44,19 @@ def test_local_patch_plans_reproduce_the_circuit(opts, golden_circuits):
     want = oracle.run(n, gates)
     got = oracle.run_plan(n, W.to_circuit(n, gates).plan_export(**opts))
     assert np.abs(got - want).max() <= 1e-12
+
+
+def test_hot_wire_relabeling_round_trip(golden_circuits):
+    """The reordering arm's relabeling on the CPU: the relabeled circuit's
+    state, with its qubit axes moved back, is the original circuit's."""
+    n = 14
+    gates = [(k, tuple(q), tuple(p)) for k, q, p in golden_circuits["local_patch_14_8_12_0x10ca1"]]
+    gates = W.relabel(gates, [n - 1 - q for q in range(n)])
+    perm = W.hot_wires_first(n, gates)
+    assert sorted(perm) == list(range(n))
+    counts = [sum(1 for _k, qs, _p in gates if len(qs) == 1 and qs[0] == q) for q in range(n)]
+    by_new = sorted(range(n), key=lambda q: perm[q])
+    assert [counts[q] for q in by_new] == sorted(counts, reverse=True)
+    st = oracle.run(n, W.relabel(gates, perm)).reshape([2] * n)
+    back = np.moveaxis(st, [n - 1 - perm[q] for q in range(n)], [n - 1 - q for q in range(n)])
+    assert np.abs(back.reshape(-1) - oracle.run(n, gates)).max() <= 1e-12

@@ -161,3 +161,48 @@ def test_graph_replay_after_buffers_swapped():
     sim.run_cached(c)                  # recaptured on the current buffer
     assert np.array_equal(sim.get_state(), first)
     assert np.abs(first - oracle.run(n, gates)).max() <= 1e-5
+
+
+def _relabel_numpy(state, n, perm):
+    """new state with qubit perm[q] holding old qubit q (LSB-first axes)."""
+    t = state.reshape([2] * n)                 # axis n-1-q is qubit q
+    src_axes = [n - 1 - q for q in range(n)]
+    dst_axes = [n - 1 - perm[q] for q in range(n)]
+    return np.moveaxis(t, src_axes, dst_axes).reshape(-1)
+
+
+@pytest.mark.parametrize("n", [2, 9, 15])
+def test_permute_qubits_matches_numpy(n):
+    rng = np.random.default_rng(40 + n)
+    init = (rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)).astype(np.complex64)
+    for trial in range(3):
+        perm = [int(x) for x in rng.permutation(n)]
+        sim = qm.Simulator(n)
+        sim.set_state(init)
+        sim.permute_qubits(perm)
+        assert np.array_equal(sim.get_state().astype(np.complex64), _relabel_numpy(init, n, perm))
+    sim = qm.Simulator(n)
+    sim.set_state(init)
+    sim.permute_qubits(list(range(n)))            # identity: nothing moves
+    assert np.array_equal(sim.get_state().astype(np.complex64), init)
+    with pytest.raises(qm.QMetalError):
+        sim.permute_qubits([0] * n)
+    with pytest.raises(qm.QMetalError):
+        sim.permute_qubits(list(range(n - 1)))
+
+
+@pytest.mark.parametrize("bits", [6, 10])
+def test_relabeled_blocked_runs_restore_the_state(bits, golden_circuits):
+    """The qubit-reordering arm: hot wires relabeled into the block window,
+    the relabeled circuit fused and blocked, one pass restores the order."""
+    n = 14
+    gates = [(k, tuple(q), tuple(p)) for k, q, p in golden_circuits["local_patch_14_8_12_0x10ca1"]]
+    gates = W.relabel(gates, [n - 1 - q for q in range(n)])     # the hot wires made high
+    perm = W.hot_wires_first(n, gates)
+    back = [0] * n
+    for q, p in enumerate(perm):
+        back[p] = q
+    sim = qm.Simulator(n)
+    sim.run_options(W.to_circuit(n, W.relabel(gates, perm)), block_bits=bits)
+    sim.permute_qubits(back)
+    assert np.abs(sim.get_state() - oracle.run(n, gates)).max() <= 1e-5
