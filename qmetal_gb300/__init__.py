@@ -95,6 +95,8 @@ _circuit_size = _decl("qm_circuit_size", c_size_t, c_void_p)
 _plan_size = _decl("qm_circuit_plan_size", c_size_t, c_void_p, c_int)
 _plan_export = _decl("qm_circuit_plan_export", c_size_t, c_void_p, c_int, c_int,
                      c_int, c_uint32, c_uint32, _f64p, c_size_t)
+_schedule_export = _decl("qm_schedule_export", c_size_t, c_void_p, POINTER(_Hamiltonian), c_int,
+                         c_uint32, _f64p, c_size_t)
 
 _create = _decl("qm_create", c_void_p, c_uint32)
 _destroy = _decl("qm_destroy", None, c_void_p)
@@ -289,6 +291,22 @@ class Circuit:
             raise QMetalError(_err())
         buf = (c_double * n)()
         _plan_export(*args, buf, n)
+        return list(buf)
+
+    def schedule_export(self, which: str, hamiltonian: "Hamiltonian | None" = None,
+                        tile_high: int = 4):
+        """The executor's launch schedule as the flat double list of
+        qm_schedule_export: which is "forward" (merged forward pass),
+        "backward" (block-wise adjoint sweep) or "costate" (lambda = H psi of
+        `hamiltonian`). Host only; needs no device."""
+        code = {"forward": 0, "backward": 1, "costate": 2}[which]
+        h = hamiltonian._c() if hamiltonian is not None else None
+        hp = byref(h) if h is not None else None
+        n = int(_schedule_export(self._h, hp, code, int(tile_high), None, 0))
+        if n == 0:
+            raise QMetalError(_err())
+        buf = (c_double * n)()
+        _schedule_export(self._h, hp, code, int(tile_high), buf, n)
         return list(buf)
 
 

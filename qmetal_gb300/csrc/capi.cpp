@@ -14,6 +14,7 @@
 
 #include "circuit.hpp"
 #include "batch.hpp"
+#include "schedule.hpp"
 #include "simulator.hpp"
 
 using namespace qmetal;
@@ -379,6 +380,29 @@ size_t qm_circuit_plan_export(qm_circuit c, int collapse, int diag, int zz, uint
   try {
     std::vector<double> v;
     serialise_plan(build_plan(c->c, options_of(collapse, diag, zz, group, block)), v);
+    if (out && cap) std::memcpy(out, v.data(), sizeof(double) * std::min(cap, v.size()));
+    return v.size();
+  } catch (const std::exception &e) {
+    set_error(e.what());
+    return 0;
+  }
+}
+
+size_t qm_schedule_export(qm_circuit c, const qm_hamiltonian *h, int which, uint32_t tile_high,
+                          double *out, size_t cap) {
+  if (!c || (which == 2 && !h)) {
+    set_error("null argument");
+    return 0;
+  }
+  try {
+    std::vector<double> v;
+    const uint32_t n = c->c.num_qubits;
+    switch (which) {
+      case 0: serialise_schedule(merged_schedule(build_plan(c->c, FusionOptions{})), n, v); break;
+      case 1: serialise_schedule(backward_schedule(c->c, tile_high), n, v); break;
+      case 2: serialise_schedule(costate_schedule(hamiltonian_of(h), n), v); break;
+      default: throw std::runtime_error("schedule: which must be 0, 1 or 2");
+    }
     if (out && cap) std::memcpy(out, v.data(), sizeof(double) * std::min(cap, v.size()));
     return v.size();
   } catch (const std::exception &e) {

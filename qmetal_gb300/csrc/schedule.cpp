@@ -1,0 +1,654 @@
+// schedule.cpp -- merged forward, co-state and backward-sweep schedules.
+#include "schedule.hpp"
+
+#include <algorithm>
+#include <map>
+#include <stdexcept>
+
+namespace qmetal {
+namespace {
+
+uint32_t popc(uint64_t x) { return static_cast<uint32_t>(__builtin_popcountll(x)); }
+
+constexpr uint32_t kWindowOps = 16;     // ops per window pass below 6 qubits
+constexpr uint32_t kWideWindowOps = 32;  // ops per warp-tile window pass
+constexpr uint32_t kWindowGrads = 16;   // gradients per window pass
+
+}  // namespace
+
+Affine::Affine(uint32_t n) : cols(n) {
+  for (uint32_t j = 0; j < n; j++) cols[j] = 1ull << j;
+}
+
+void Affine::then_cx(uint32_t c, uint32_t t) {
+  auto f = [&](uint64_t v) { return v ^ (((v >> c) & 1ull) << t); };
+  for (uint64_t &v : cols) v = f(v);
+  off = f(off);
+}
+
+void Affine::then_swap(uint32_t a, uint32_t b) {
+  auto f = [&](uint64_t v) {
+    const uint64_t d = ((v >> a) ^ (v >> b)) & 1ull;
+    return v ^ (d << a) ^ (d << b);
+  };
+  for (uint64_t &v : cols) v = f(v);
+  off = f(off);
+}
+
+uint32_t Affine::sectors() const {
+  std::vector<uint64_t> s;
+  for (uint64_t y = 0; y < 64 && y < (1ull << cols.size()); y++) {
+    uint64_t x = off;
+    for (uint32_t j = 0; j < cols.size() && j < 6; j++)
+      if ((y >> j) & 1) x ^= cols[j];
+    s.push_back(x >> 2);
+  }
+  std::sort(s.begin(), s.end());
+  return static_cast<uint32_t>(std::unique(s.begin(), s.end()) - s.begin());
+}
+
+// Every gate of a run is an involution, so undoing the run composes its gates
+// first to last, and applying it composes them last to first.
+Affine run_map(uint32_t n, const std::vector<PermGate> &run, bool undo) {
+  Affine m(n);
+  auto step = [&](const PermGate &g) {
+    if (g.swap) m.then_swap(g.a, g.b);
+    else m.then_cx(g.a, g.b);
+  };
+  if (undo) {
+    for (const PermGate &g : run) step(g);
+  } else {
+    for (size_t k = run.size(); k-- > 0;) step(run[k]);
+  }
+  return m;
+}
+
+// A gather pass moves 2S, more when the warp's sources scatter; the run's
+// gates move S each (half the state read and written per CX, all of it
+// crossing for a SWAP, counted as S by the roofline model).
+bool permutation_pays(const Affine &m, size_t gates) {
+  const double pass = 2.0 * std::max(1.0, m.sectors() / 16.0);
+  return pass * 1.25 < static_cast<double>(gates);
+}
+
+Gate invert(const Gate &g) {
+  Gate inv = g;
+  switch (g.kind) {
+    case G_RX: case G_RY: case G_RZ: case G_P: case G_CP:
+      inv.params[0] = -g.params[0];
+      break;
+    case G_S: inv.kind = G_SDG; break;
+    case G_SDG: inv.kind = G_S; break;
+    case G_T: inv.kind = G_TDG; break;
+    case G_TDG: inv.kind = G_T; break;
+    case G_U3:   // U3(t, f, l)^-1 = U3(-t, -l, -f)
+      inv.params[0] = -g.params[0];
+      inv.params[1] = -g.params[2];
+      inv.params[2] = -g.params[1];
+      break;
+    default: break;
+  }
+  return inv;
+}
+
+int generator_of(const Gate &g) {
+  switch (g.kind) {
+    case G_RX: return 1;
+    case G_RY: return 2;
+    case G_RZ: return 3;
+    default: return 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+
+std::vector<ForwardStep> merged_schedule(const Plan &p) {
+  const uint32_t n = p.num_qubits;
+  std::vector<ForwardStep> out;
+  std::vector<uint32_t> wires;
+  std::vector<cdouble> mats;
+  auto fits = [&](const std::vector<uint32_t> &w) {
+    uint32_t lane = 0, high = 0, zero = 0;
+    for (uint32_t q : w) {
+      if (q == 0) zero++;
+      else if (q <= 5) lane++;
+      else high++;
+    }
+    if (zero > 1) return false;
+    if (lane >= 1 && lane <= 5 && high <= 4 && n >= 6 + high) return true;
+    return lane + high <= 5;
+  };
+  auto flush = [&]() {
+    if (wires.empty()) return;
+    std::vector<size_t> order(wires.size());
+    for (size_t i = 0; i < order.size(); i++) order[i] = i;
+    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return wires[a] < wires[b]; });
+    ForwardStep s;
+    s.kind = ForwardStep::Group;
+    for (size_t i : order) {
+      s.wires.push_back(wires[i]);
+      s.mats.insert(s.mats.end(), mats.begin() + 4 * i, mats.begin() + 4 * i + 4);
+    }
+    out.push_back(std::move(s));
+    wires.clear();
+    mats.clear();
+  };
+  std::vector<PermGate> run;
+  std::vector<size_t> run_ops;
+  auto flush_run = [&]() {
+    if (run.empty()) return;
+    const Affine map = run.size() >= 2 ? run_map(n, run, false) : Affine(0);
+    if (run.size() >= 2 && permutation_pays(map, run.size())) {
+      ForwardStep s;
+      s.kind = ForwardStep::Permute;
+      s.cols = map.cols;
+      s.off = map.off;
+      s.ops = run_ops;
+      out.push_back(std::move(s));
+    } else {
+      for (size_t i : run_ops) {
+        ForwardStep s;
+        s.ops = {i};
+        out.push_back(std::move(s));
+      }
+    }
+    run.clear();
+    run_ops.clear();
+  };
+  for (size_t i = 0; i < p.ops.size(); i++) {
+    const PlanOp &op = p.ops[i];
+    const bool cx = op.kind == PlanOp::Kind::Controlled1q && op.matrix[0] == 0.0 &&
+                    op.matrix[1] == 1.0 && op.matrix[2] == 1.0 && op.matrix[3] == 0.0;
+    if ((cx || op.kind == PlanOp::Kind::Swap) && op.qubits[0] < n && op.qubits[1] < n &&
+        op.qubits[0] != op.qubits[1]) {
+      flush();
+      run.push_back({op.kind == PlanOp::Kind::Swap, op.qubits[0], op.qubits[1]});
+      run_ops.push_back(i);
+      continue;
+    }
+    flush_run();
+    std::vector<uint32_t> w;
+    std::vector<cdouble> m;
+    if (op.kind == PlanOp::Kind::Dense1q) {
+      w.push_back(op.qubits[0]);
+      m.assign(op.matrix, op.matrix + 4);
+    } else if (op.kind == PlanOp::Kind::Dense1qGroup) {
+      w = op.group_qubits;
+      m = op.group_matrices;
+    } else {
+      flush();
+      ForwardStep s;
+      s.ops = {i};
+      out.push_back(std::move(s));
+      continue;
+    }
+    for (uint32_t q : w)
+      if (q >= n) throw std::runtime_error("qubit index out of range");
+    bool overlap = false;
+    for (uint32_t q : w)
+      if (std::find(wires.begin(), wires.end(), q) != wires.end()) overlap = true;
+    if (overlap) flush();
+    // The group's wires commute with each other and with the pending ones,
+    // so they join the pass one by one and spill into the next when it is
+    // full.
+    for (size_t j = 0; j < w.size(); j++) {
+      std::vector<uint32_t> trial = wires;
+      trial.push_back(w[j]);
+      if (!fits(trial)) flush();
+      wires.push_back(w[j]);
+      mats.insert(mats.end(), m.begin() + 4 * j, m.begin() + 4 * j + 4);
+    }
+  }
+  flush();
+  flush_run();
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+
+namespace {
+
+struct FlipGroup {
+  uint64_t flip;
+  std::vector<size_t> terms;
+};
+
+std::vector<FlipGroup> group_by_flip(const std::vector<const PauliTerm *> &terms) {
+  std::vector<FlipGroup> out;
+  std::map<uint64_t, size_t> where;
+  for (size_t t = 0; t < terms.size(); t++) {
+    const PauliString &p = terms[t]->pauli;
+    const uint64_t f = p.x_mask | p.y_mask;
+    auto it = where.find(f);
+    if (it == where.end()) {
+      where[f] = out.size();
+      out.push_back({f, {t}});
+    } else {
+      out[it->second].terms.push_back(t);
+    }
+  }
+  return out;
+}
+
+}  // namespace
+
+// Z strings of <= 2 bits go as one quadratic-form pass; terms that flip one
+// wire pack many wires per pass (wires 0..5 ride along in every pass, at most
+// four wires >= 6 and 16 terms a pass); anything else goes one pass per flip
+// mask, 16 terms at a time. A Hamiltonian of only short Z strings needs no
+// separate energy pass.
+std::vector<CostateStep> costate_schedule(const Hamiltonian &h, uint32_t n) {
+  std::vector<CostateStep> out;
+  bool zonly = !h.terms.empty();
+  for (const PauliTerm &t : h.terms)
+    if (t.pauli.x_mask | t.pauli.y_mask || popc(t.pauli.z_mask) > 2) zonly = false;
+  std::vector<const PauliTerm *> zpart, local, rest;
+  for (const PauliTerm &t : h.terms) {
+    const uint64_t flip = t.pauli.x_mask | t.pauli.y_mask;
+    if (!flip && popc(t.pauli.z_mask) <= 2) zpart.push_back(&t);
+    else if (popc(flip) == 1 && n >= 6) local.push_back(&t);
+    else rest.push_back(&t);
+  }
+  bool first = true;
+  if (!zpart.empty()) {
+    CostateStep s;
+    s.kind = CostateStep::ZDiag;
+    s.overwrite = true;
+    for (const PauliTerm *t : zpart) {
+      s.masks.push_back(t->pauli.z_mask);
+      s.coeffs.push_back(t->coefficient);
+    }
+    out.push_back(std::move(s));
+    first = false;
+    if (zonly) return out;
+  }
+  if (!local.empty()) {
+    auto wire_of = [&](const PauliTerm *t) {
+      return static_cast<uint32_t>(__builtin_ctzll(t->pauli.x_mask | t->pauli.y_mask));
+    };
+    std::stable_sort(local.begin(), local.end(),
+                     [&](const PauliTerm *a, const PauliTerm *b) { return wire_of(a) < wire_of(b); });
+    const uint32_t max_high = std::min<uint32_t>(4, n - 6);
+    CostateStep s;
+    std::vector<uint32_t> highs;
+    auto flush = [&]() {
+      if (s.wires.empty()) return;
+      s.kind = CostateStep::Local;
+      s.overwrite = first;
+      first = false;
+      out.push_back(std::move(s));
+      s = CostateStep{};
+      highs.clear();
+    };
+    for (const PauliTerm *t : local) {
+      const uint32_t w = wire_of(t);
+      const bool new_high = w >= 6 && std::find(highs.begin(), highs.end(), w) == highs.end();
+      if (s.wires.size() == kCostateTermsPerPass || (new_high && highs.size() == max_high)) flush();
+      if (w >= 6 && std::find(highs.begin(), highs.end(), w) == highs.end()) highs.push_back(w);
+      s.wires.push_back(w);
+      s.masks.push_back(t->pauli.y_mask | t->pauli.z_mask);
+      s.nys.push_back(popc(t->pauli.y_mask));
+      s.coeffs.push_back(t->coefficient);
+    }
+    flush();
+  }
+  for (const FlipGroup &g : group_by_flip(rest)) {
+    for (size_t b = 0; b < g.terms.size(); b += kCostateTermsPerPass) {
+      const size_t take = std::min<size_t>(kCostateTermsPerPass, g.terms.size() - b);
+      CostateStep s;
+      s.kind = CostateStep::Flip;
+      s.overwrite = first;
+      s.flip = g.flip;
+      for (size_t j = 0; j < take; j++) {
+        const PauliTerm &t = *rest[g.terms[b + j]];
+        s.masks.push_back(t.pauli.y_mask | t.pauli.z_mask);
+        s.nys.push_back(popc(t.pauli.y_mask));
+        s.coeffs.push_back(t.coefficient);
+      }
+      out.push_back(std::move(s));
+      first = false;
+    }
+  }
+  if (first) out.push_back(CostateStep{});
+  CostateStep dot;
+  dot.kind = CostateStep::Dot;
+  out.push_back(std::move(dot));
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+
+namespace {
+
+// A run of the circuit that the sweep undoes as a unit.
+struct Segment {
+  enum Kind { Window, Diag, Single } kind = Single;
+  size_t begin = 0, end = 0;
+  bool has_param = false;
+  // Diag: the block's forward phase terms and its Z-string generators.
+  std::vector<uint64_t> masks;
+  std::vector<double> angles;
+  double gphase = 0.0;
+  std::vector<uint64_t> gens;
+  std::vector<uint32_t> slots;
+};
+
+// Forward segmentation: a maximal run of one-qubit gates is a window; a run
+// of ZZ couplings (CX.RZ.CX) and two-qubit diagonal gates is a diagonal block;
+// anything else stands alone.
+std::vector<Segment> segment_circuit(const Circuit &c) {
+  std::vector<Segment> segs;
+  const size_t G = c.ops.size();
+  size_t i = 0;
+  while (i < G) {
+    const Gate &g = c.ops[i];
+    Segment s;
+    s.begin = i;
+    uint32_t a, b;
+    double t;
+    if (g.num_qubits == 1) {
+      s.kind = Segment::Window;
+      size_t j = i;
+      for (; j < G && c.ops[j].num_qubits == 1; j++)
+        if (c.ops[j].num_params) s.has_param = true;
+      s.end = j;
+    } else if (zz_coupling_at(c, i, &a, &b, &t) || (g.num_qubits == 2 && is_diagonal(g))) {
+      s.kind = Segment::Diag;
+      size_t j = i;
+      while (j < G) {
+        if (zz_coupling_at(c, j, &a, &b, &t)) {
+          const uint64_t ma = 1ull << a, mb = 1ull << b;
+          s.masks.insert(s.masks.end(), {ma, mb, ma | mb});
+          s.angles.insert(s.angles.end(), {t, t, -2.0 * t});
+          s.gphase += -t / 2.0;
+          if (c.ops[j + 1].num_params) {
+            s.gens.push_back(ma | mb);   // exp(-i t/2 Z_a Z_b)
+            s.slots.push_back(static_cast<uint32_t>(j + 1));
+            s.has_param = true;
+          }
+          j += 3;
+        } else if (c.ops[j].num_qubits == 2 && is_diagonal(c.ops[j])) {
+          s.gphase += diagonal_term(c.ops[j], s.masks, s.angles);
+          if (c.ops[j].num_params) s.has_param = true;
+          j++;
+        } else {
+          break;
+        }
+      }
+      s.end = j;
+    } else {
+      s.kind = Segment::Single;
+      s.end = i + 1;
+      s.has_param = g.num_params > 0;
+    }
+    i = s.end;
+    segs.push_back(std::move(s));
+  }
+  return segs;
+}
+
+}  // namespace
+
+// Every gradient of a commuting block is read at the block boundary and the
+// block is undone on both states in the same pass. Blocks before the first
+// parameterised one are never undone.
+std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high) {
+  const uint32_t n = c.num_qubits;
+  tile_high = std::min<uint32_t>(std::max<uint32_t>(tile_high, 1), 4);
+  std::vector<BackwardStep> out;
+  const auto segs = segment_circuit(c);
+  size_t first = segs.size();
+  for (size_t s = 0; s < segs.size(); s++)
+    if (segs[s].has_param) {
+      first = s;
+      break;
+    }
+  for (size_t s = segs.size(); s-- > first;) {
+    const Segment &seg = segs[s];
+    const bool undo = s > first;
+    if (seg.kind == Segment::Single) {
+      // A run of CX / SWAP gates, all undone here, goes as one gather pass
+      // per state when that moves fewer bytes.
+      auto perm_gate = [&](size_t k) {
+        const Gate &g = c.ops[segs[k].begin];
+        return segs[k].kind == Segment::Single && (g.kind == G_CX || g.kind == G_SWAP) &&
+               g.qubits[0] < n && g.qubits[1] < n && g.qubits[0] != g.qubits[1];
+      };
+      if (undo && perm_gate(s)) {
+        size_t lo = s;
+        while (lo - 1 > first && perm_gate(lo - 1)) lo--;
+        if (s > lo) {
+          std::vector<PermGate> run;
+          for (size_t k = lo; k <= s; k++) {
+            const Gate &g = c.ops[segs[k].begin];
+            run.push_back({g.kind == G_SWAP, g.qubits[0], g.qubits[1]});
+          }
+          const Affine map = run_map(n, run, true);
+          if (permutation_pays(map, run.size())) {
+            BackwardStep st;
+            st.kind = BackwardStep::PermuteUndo;
+            st.cols = map.cols;
+            st.off = map.off;
+            for (size_t k = s + 1; k-- > lo;) st.gates.push_back(segs[k].begin);
+            out.push_back(std::move(st));
+            s = lo;
+            continue;
+          }
+        }
+      }
+      if (undo) {
+        BackwardStep st;
+        st.gates = {seg.begin};
+        out.push_back(std::move(st));
+      }
+      continue;
+    }
+    if (seg.kind == Segment::Diag) {
+      const uint32_t ng = static_cast<uint32_t>(seg.gens.size());
+      if (ng == 0 && !undo) continue;
+      uint32_t done = 0;
+      do {
+        const uint32_t take = std::min(kDiagGensPerPass, ng - done);
+        BackwardStep st;
+        st.kind = BackwardStep::Diag;
+        st.masks = seg.masks;
+        st.angles = seg.angles;
+        st.gphase = seg.gphase;
+        st.gens.assign(seg.gens.begin() + done, seg.gens.begin() + done + take);
+        st.slots.assign(seg.slots.begin() + done, seg.slots.begin() + done + take);
+        st.undo = done + take == ng && undo;
+        out.push_back(std::move(st));
+        done += take;
+      } while (done < ng);
+      continue;
+    }
+    // Window: each wire's gates last to first, a few wires per pass. Gates
+    // on different wires commute, and a generator on one wire commutes with
+    // every gate on the others, so the order across wires is free.
+    std::vector<std::vector<size_t>> per_wire(n);
+    for (size_t k = seg.begin; k < seg.end; k++) per_wire[c.ops[k].qubits[0]].push_back(k);
+    std::vector<WireOp> tile;
+    uint32_t others = 0, highs = 0, grads = 0;
+    bool tile_has_param = false;
+    const bool wide = n >= 6;
+    const uint32_t max_ops = wide ? kWideWindowOps : kWindowOps;
+    const uint32_t max_high = wide ? std::min<uint32_t>(tile_high, n - 6) : 0;
+    auto flush = [&]() {
+      if (tile.empty()) return;
+      if (undo || tile_has_param) {
+        BackwardStep st;
+        st.kind = BackwardStep::Window;
+        st.tile = tile;
+        out.push_back(std::move(st));
+      }
+      tile.clear();
+      others = highs = grads = 0;
+      tile_has_param = false;
+    };
+    for (uint32_t w = 0; w < n; w++) {
+      if (per_wire[w].empty()) continue;
+      std::vector<WireOp> ops;
+      uint32_t wgrads = 0;
+      for (size_t r = per_wire[w].size(); r-- > 0;) {
+        const size_t k = per_wire[w][r];
+        const Gate &g = c.ops[k];
+        const Gate inv = invert(g);
+        WireOp o{};
+        o.wire = w;
+        gate_matrix_1q(inv.kind, inv.params, o.minv);
+        o.gen = g.num_params > 0 ? generator_of(g) : 0;
+        o.slot = static_cast<uint32_t>(k);
+        if (o.gen) wgrads++;
+        ops.push_back(o);
+      }
+      const uint32_t need_other = w != 0 ? 1u : 0u, need_high = w >= 6 ? 1u : 0u;
+      if (ops.size() > max_ops || wgrads > kWindowGrads) {
+        flush();
+        for (size_t b = 0; b < ops.size(); b += kWindowOps) {
+          const size_t e = std::min<size_t>(ops.size(), b + kWindowOps);
+          tile.assign(ops.begin() + b, ops.begin() + e);
+          for (const WireOp &o : tile) tile_has_param |= o.gen != 0;
+          flush();
+        }
+        continue;
+      }
+      bool full;
+      if (wide) {
+        // Warp tiles: wire 0, wires 1..5 in the lanes, up to four wires >= 6.
+        full = tile.size() + ops.size() > max_ops || highs + need_high > max_high ||
+               grads + wgrads > kWindowGrads;
+      } else {
+        const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;
+        full = tile.size() + ops.size() > kWindowOps || others + need_other > 3 ||
+               grads + wgrads > cap;
+      }
+      if (full) flush();
+      tile.insert(tile.end(), ops.begin(), ops.end());
+      others += need_other;
+      highs += need_high;
+      grads += wgrads;
+      tile_has_param |= wgrads > 0;
+    }
+    flush();
+  }
+  return out;
+}
+
+// ---------------------------------------------------------------------------
+
+namespace {
+
+void put_map(std::vector<double> &v, uint32_t n, const std::vector<uint64_t> &cols, uint64_t off) {
+  v.push_back(n);
+  for (uint32_t j = 0; j < n; j++) v.push_back(static_cast<double>(cols[j]));
+  v.push_back(static_cast<double>(off));
+}
+
+void put_mat(std::vector<double> &v, const cdouble *m) {
+  for (int k = 0; k < 4; k++) {
+    v.push_back(m[k].real());
+    v.push_back(m[k].imag());
+  }
+}
+
+}  // namespace
+
+void serialise_schedule(const std::vector<ForwardStep> &s, uint32_t n, std::vector<double> &v) {
+  v.push_back(static_cast<double>(s.size()));
+  for (const ForwardStep &st : s) {
+    v.push_back(st.kind);
+    if (st.kind == ForwardStep::Group) {
+      v.push_back(static_cast<double>(st.wires.size()));
+      for (size_t i = 0; i < st.wires.size(); i++) {
+        v.push_back(st.wires[i]);
+        put_mat(v, &st.mats[4 * i]);
+      }
+    } else if (st.kind == ForwardStep::Permute) {
+      put_map(v, n, st.cols, st.off);
+      v.push_back(static_cast<double>(st.ops.size()));
+      for (size_t i : st.ops) v.push_back(static_cast<double>(i));
+    } else {
+      v.push_back(static_cast<double>(st.ops.at(0)));
+    }
+  }
+}
+
+void serialise_schedule(const std::vector<CostateStep> &s, std::vector<double> &v) {
+  v.push_back(static_cast<double>(s.size()));
+  for (const CostateStep &st : s) {
+    v.push_back(st.kind);
+    switch (st.kind) {
+      case CostateStep::ZDiag:
+        v.push_back(static_cast<double>(st.masks.size()));
+        for (size_t i = 0; i < st.masks.size(); i++) {
+          v.push_back(static_cast<double>(st.masks[i]));
+          v.push_back(st.coeffs[i]);
+        }
+        break;
+      case CostateStep::Local:
+        v.push_back(st.overwrite ? 1.0 : 0.0);
+        v.push_back(static_cast<double>(st.wires.size()));
+        for (size_t i = 0; i < st.wires.size(); i++) {
+          v.push_back(st.wires[i]);
+          v.push_back(static_cast<double>(st.masks[i]));
+          v.push_back(st.nys[i]);
+          v.push_back(st.coeffs[i]);
+        }
+        break;
+      case CostateStep::Flip:
+        v.push_back(st.overwrite ? 1.0 : 0.0);
+        v.push_back(static_cast<double>(st.flip));
+        v.push_back(static_cast<double>(st.masks.size()));
+        for (size_t i = 0; i < st.masks.size(); i++) {
+          v.push_back(static_cast<double>(st.masks[i]));
+          v.push_back(st.nys[i]);
+          v.push_back(st.coeffs[i]);
+        }
+        break;
+      default:
+        break;
+    }
+  }
+}
+
+void serialise_schedule(const std::vector<BackwardStep> &s, uint32_t n, std::vector<double> &v) {
+  v.push_back(static_cast<double>(s.size()));
+  for (const BackwardStep &st : s) {
+    v.push_back(st.kind);
+    switch (st.kind) {
+      case BackwardStep::Window:
+        v.push_back(static_cast<double>(st.tile.size()));
+        for (const WireOp &o : st.tile) {
+          v.push_back(o.wire);
+          put_mat(v, o.minv);
+          v.push_back(o.gen);
+          v.push_back(o.slot);
+        }
+        break;
+      case BackwardStep::Diag:
+        v.push_back(st.undo ? 1.0 : 0.0);
+        v.push_back(static_cast<double>(st.masks.size()));
+        for (size_t i = 0; i < st.masks.size(); i++) {
+          v.push_back(static_cast<double>(st.masks[i]));
+          v.push_back(st.angles[i]);
+        }
+        v.push_back(st.gphase);
+        v.push_back(static_cast<double>(st.gens.size()));
+        for (size_t i = 0; i < st.gens.size(); i++) {
+          v.push_back(static_cast<double>(st.gens[i]));
+          v.push_back(st.slots[i]);
+        }
+        break;
+      case BackwardStep::PermuteUndo:
+        put_map(v, n, st.cols, st.off);
+        v.push_back(static_cast<double>(st.gates.size()));
+        for (size_t g : st.gates) v.push_back(static_cast<double>(g));
+        break;
+      case BackwardStep::GateUndo:
+        v.push_back(static_cast<double>(st.gates.at(0)));
+        break;
+    }
+  }
+}
+
+}  // namespace qmetal

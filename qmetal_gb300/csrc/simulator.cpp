@@ -18,6 +18,7 @@
 #include <stdexcept>
 
 #include "../../include/qmetal/qmetal_kernels.h"
+#include "schedule.hpp"
 
 namespace qmetal {
 namespace {
@@ -50,103 +51,7 @@ void cuda_check(cudaError_t e, const char *what) {
   if (e != cudaSuccess) throw std::runtime_error(std::string(what) + ": " + cudaGetErrorString(e));
 }
 
-// The reference's invert() (src/metal/simulator.mm:786-799).
-Gate invert(const Gate &g) {
-  Gate inv = g;
-  switch (g.kind) {
-    case G_RX: case G_RY: case G_RZ: case G_P: case G_CP:
-      inv.params[0] = -g.params[0];
-      break;
-    case G_S: inv.kind = G_SDG; break;
-    case G_SDG: inv.kind = G_S; break;
-    case G_T: inv.kind = G_TDG; break;
-    case G_TDG: inv.kind = G_T; break;
-    case G_U3:   // U3(t, f, l)^-1 = U3(-t, -l, -f)
-      inv.params[0] = -g.params[0];
-      inv.params[1] = -g.params[2];
-      inv.params[2] = -g.params[1];
-      break;
-    default: break;
-  }
-  return inv;
-}
-
-// Generator code of a natively differentiable rotation: 1 X, 2 Y, 3 Z.
-int generator_of(const Gate &g) {
-  switch (g.kind) {
-    case G_RX: return 1;
-    case G_RY: return 2;
-    case G_RZ: return 3;
-    default: return 0;
-  }
-}
-
 uint32_t popc(uint64_t x) { return static_cast<uint32_t>(__builtin_popcountll(x)); }
-
-// x -> A x ^ off over GF(2); cols[j] = A e_j.
-struct Affine {
-  std::vector<uint64_t> cols;
-  uint64_t off = 0;
-  explicit Affine(uint32_t n) : cols(n) {
-    for (uint32_t j = 0; j < n; j++) cols[j] = 1ull << j;
-  }
-  // Compose g after the map: x -> g(A x ^ off), g a CX (c, t) or a SWAP (a, b).
-  void then_cx(uint32_t c, uint32_t t) {
-    auto f = [&](uint64_t v) { return v ^ (((v >> c) & 1ull) << t); };
-    for (uint64_t &v : cols) v = f(v);
-    off = f(off);
-  }
-  void then_swap(uint32_t a, uint32_t b) {
-    auto f = [&](uint64_t v) {
-      const uint64_t d = ((v >> a) ^ (v >> b)) & 1ull;
-      return v ^ (d << a) ^ (d << b);
-    };
-    for (uint64_t &v : cols) v = f(v);
-    off = f(off);
-  }
-  // Distinct 32-byte sectors a warp's 64 sources touch (16 when contiguous).
-  uint32_t sectors() const {
-    std::vector<uint64_t> s;
-    for (uint64_t y = 0; y < 64 && y < (1ull << cols.size()); y++) {
-      uint64_t x = off;
-      for (uint32_t j = 0; j < cols.size() && j < 6; j++)
-        if ((y >> j) & 1) x ^= cols[j];
-      s.push_back(x >> 2);
-    }
-    std::sort(s.begin(), s.end());
-    return static_cast<uint32_t>(std::unique(s.begin(), s.end()) - s.begin());
-  }
-};
-
-// One gate of a permutation run: CX (control, target) or SWAP (a, b).
-struct PermGate {
-  bool swap;
-  uint32_t a, b;
-};
-
-// Gather map for a run applied forward (x -> F(x), so dst[y] = src[F^-1(y)])
-// or undone (dst[y] = src[F(y)]); every gate of the run is an involution.
-Affine run_map(uint32_t n, const std::vector<PermGate> &run, bool undo) {
-  Affine m(n);
-  auto step = [&](const PermGate &g) {
-    if (g.swap) m.then_swap(g.a, g.b);
-    else m.then_cx(g.a, g.b);
-  };
-  if (undo) {
-    for (const PermGate &g : run) step(g);
-  } else {
-    for (size_t k = run.size(); k-- > 0;) step(run[k]);
-  }
-  return m;
-}
-
-// A gather pass moves 2S, more when the warp's sources scatter; the run's
-// gates move S each (half the state read and written per CX, all of it
-// crossing for a SWAP, counted as S by the roofline model).
-bool permutation_pays(const Affine &m, size_t gates) {
-  const double pass = 2.0 * std::max(1.0, m.sectors() / 16.0);
-  return pass * 1.25 < static_cast<double>(gates);
-}
 
 struct FlipGroup {
   uint64_t flip;
@@ -476,104 +381,32 @@ void Simulator::run_cached(const Circuit &c) {
   cuda_check(cudaGraphLaunch(exec, S(stream_)), "graph launch");
 }
 
-// The plan with consecutive one-qubit ops merged into wider group passes.
-// The plan emits a window's 2x2 products as Dense1q / Dense1qGroup ops on
-// distinct wires, which commute, so any set of them can share one pass: wire
-// 0, up to five of wires 1..5 (warp shuffles) and four wires >= 6
-// (registers), or wire 0 and five wires >= 1 in registers.
+// The plan through merged_schedule(): one group pass per merged set of
+// one-qubit ops, one gather pass per CX / SWAP run that pays, the plan's op
+// kernel for everything else.
 void Simulator::run_merged(const Plan &p) {
   if (p.num_qubits != n_) throw std::runtime_error("plan/simulator size mismatch");
   activate();
-  std::vector<uint32_t> wires;
-  std::vector<cdouble> mats;
-  auto fits = [&](const std::vector<uint32_t> &w) {
-    uint32_t lane = 0, high = 0, zero = 0;
-    for (uint32_t q : w) {
-      if (q == 0) zero++;
-      else if (q <= 5) lane++;
-      else high++;
-    }
-    if (zero > 1) return false;
-    if (lane >= 1 && lane <= 5 && high <= 4 && n_ >= 6 + high) return true;
-    return lane + high <= 5;
-  };
-  auto flush = [&]() {
-    if (wires.empty()) return;
-    std::vector<size_t> order(wires.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = i;
-    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return wires[a] < wires[b]; });
-    std::vector<uint32_t> ws;
-    std::vector<float> fm(8 * wires.size());
-    for (size_t i = 0; i < order.size(); i++) {
-      ws.push_back(wires[order[i]]);
-      narrow(&mats[4 * order[i]], &fm[8 * i]);
-    }
-    check(qmk_apply_group(state_, n_, static_cast<uint32_t>(ws.size()), ws.data(), fm.data(),
-                          stream_),
-          "merged group");
-    dispatches_++;
-    wires.clear();
-    mats.clear();
-  };
-  // Consecutive CX / SWAP ops: one permutation pass when that moves fewer
-  // bytes than the ops one by one.
-  std::vector<PermGate> run;
-  std::vector<const PlanOp *> run_ops;
-  auto flush_run = [&]() {
-    if (run.empty()) return;
-    bool done = false;
-    if (run.size() >= 2) {
-      const Affine map = run_map(n_, run, false);
-      if (permutation_pays(map, run.size())) done = permute(state_, map.cols, map.off);
-    }
-    if (!done)
-      for (const PlanOp *o : run_ops) apply_op_to(state_, *o);
-    run.clear();
-    run_ops.clear();
-  };
-  for (const PlanOp &op : p.ops) {
-    const bool cx = op.kind == PlanOp::Kind::Controlled1q && op.matrix[0] == 0.0 &&
-                    op.matrix[1] == 1.0 && op.matrix[2] == 1.0 && op.matrix[3] == 0.0;
-    if ((cx || op.kind == PlanOp::Kind::Swap) && op.qubits[0] < n_ && op.qubits[1] < n_ &&
-        op.qubits[0] != op.qubits[1]) {
-      flush();
-      run.push_back({op.kind == PlanOp::Kind::Swap, op.qubits[0], op.qubits[1]});
-      run_ops.push_back(&op);
-      continue;
-    }
-    flush_run();
-    std::vector<uint32_t> w;
-    std::vector<cdouble> m;
-    if (op.kind == PlanOp::Kind::Dense1q) {
-      w.push_back(op.qubits[0]);
-      m.assign(op.matrix, op.matrix + 4);
-    } else if (op.kind == PlanOp::Kind::Dense1qGroup) {
-      w = op.group_qubits;
-      m = op.group_matrices;
-    } else {
-      flush();
-      apply_op_to(state_, op);
-      continue;
-    }
-    for (uint32_t q : w)
-      if (q >= n_) throw std::runtime_error("qubit index out of range");
-    bool overlap = false;
-    for (uint32_t q : w)
-      if (std::find(wires.begin(), wires.end(), q) != wires.end()) overlap = true;
-    if (overlap) flush();
-    // The group's wires commute with each other and with the pending ones,
-    // so they join the pass one by one and spill into the next when it is
-    // full.
-    for (size_t j = 0; j < w.size(); j++) {
-      std::vector<uint32_t> trial = wires;
-      trial.push_back(w[j]);
-      if (!fits(trial)) flush();
-      wires.push_back(w[j]);
-      mats.insert(mats.end(), m.begin() + 4 * j, m.begin() + 4 * j + 4);
+  for (const ForwardStep &st : merged_schedule(p)) {
+    switch (st.kind) {
+      case ForwardStep::Group: {
+        std::vector<float> fm(2 * st.mats.size());
+        for (size_t i = 0; i < st.wires.size(); i++) narrow(&st.mats[4 * i], &fm[8 * i]);
+        check(qmk_apply_group(state_, n_, static_cast<uint32_t>(st.wires.size()), st.wires.data(),
+                              fm.data(), stream_),
+              "merged group");
+        dispatches_++;
+        break;
+      }
+      case ForwardStep::Permute:
+        if (!permute(state_, st.cols, st.off))
+          for (size_t i : st.ops) apply_op_to(state_, p.ops[i]);
+        break;
+      case ForwardStep::Op:
+        apply_op_to(state_, p.ops[st.ops[0]]);
+        break;
     }
   }
-  flush();
-  flush_run();
 }
 
 void Simulator::permute_qubits(const std::vector<uint32_t> &perm) {
@@ -944,118 +777,40 @@ void Simulator::prepare_adjoint(const Circuit &c, const Hamiltonian &h) {
   cuda_check(cudaMemsetAsync(d_grad_, 0, G * sizeof(double), S(stream_)), "gradient zero");
 }
 
-// lambda = H psi and E = <psi|H|psi> into d_results_[0]. A Hamiltonian of Z
-// strings of weight <= 2 takes one fused pass; anything else goes term group
-// by term group, then a dot product.
+// lambda = H psi and E = <psi|H|psi> into d_results_[0], through
+// costate_schedule().
 double Simulator::energy_and_costate(const Hamiltonian &h) {
-  bool zonly = !h.terms.empty();
-  std::vector<uint64_t> zm;
-  std::vector<double> zc;
-  for (const PauliTerm &t : h.terms) {
-    if (t.pauli.x_mask | t.pauli.y_mask || popc(t.pauli.z_mask) > 2) zonly = false;
-    zm.push_back(t.pauli.z_mask);
-    zc.push_back(t.coefficient);
-  }
-  if (zonly) {
-    check(qmk_zdiag_costate(costate_, state_, n_, static_cast<uint32_t>(zm.size()), zm.data(),
-                            zc.data(), d_results_, ws_, ws_bytes_, stream_),
-          "co-state");
-    dispatches_ += 2;
-    return 0.0;
-  }
-  // Mixed Hamiltonian: Z strings of <= 2 bits as one quadratic-form pass,
-  // terms that flip one wire many wires per pass, anything else one pass per
-  // flip mask; then the energy Re<psi|lambda>.
-  Hamiltonian zpart, local, rest;
-  for (const PauliTerm &t : h.terms) {
-    const uint64_t flip = t.pauli.x_mask | t.pauli.y_mask;
-    if (!flip && popc(t.pauli.z_mask) <= 2) zpart.terms.push_back(t);
-    else if (popc(flip) == 1 && n_ >= 6) local.terms.push_back(t);
-    else rest.terms.push_back(t);
-  }
-  bool first = true;
-  if (!zpart.terms.empty()) {
-    zm.clear();
-    zc.clear();
-    for (const PauliTerm &t : zpart.terms) {
-      zm.push_back(t.pauli.z_mask);
-      zc.push_back(t.coefficient);
-    }
-    check(qmk_zdiag_costate(costate_, state_, n_, static_cast<uint32_t>(zm.size()), zm.data(),
-                            zc.data(), d_results_, ws_, ws_bytes_, stream_),
-          "co-state");
-    dispatches_ += 2;
-    first = false;
-  }
-  if (!local.terms.empty()) {
-    // Tiles: wires 0..5 ride along in every pass; at most four wires >= 6
-    // and 16 terms per pass.
-    std::vector<size_t> order(local.terms.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = i;
-    auto wire_of = [&](size_t i) {
-      const PauliString &p = local.terms[i].pauli;
-      return static_cast<uint32_t>(__builtin_ctzll(p.x_mask | p.y_mask));
-    };
-    std::stable_sort(order.begin(), order.end(),
-                     [&](size_t a, size_t b) { return wire_of(a) < wire_of(b); });
-    const uint32_t max_high = std::min<uint32_t>(4, n_ - 6);
-    std::vector<uint32_t> wires, nys;
-    std::vector<uint64_t> signs;
-    std::vector<double> coeffs;
-    std::vector<uint32_t> highs;
-    auto flush = [&]() {
-      if (wires.empty()) return;
-      check(qmk_pauli_accum_local(costate_, state_, n_, static_cast<uint32_t>(wires.size()),
-                                  wires.data(), signs.data(), nys.data(), coeffs.data(),
-                                  first ? 1 : 0, stream_),
-            "co-state");
-      dispatches_++;
-      first = false;
-      wires.clear();
-      nys.clear();
-      signs.clear();
-      coeffs.clear();
-      highs.clear();
-    };
-    for (size_t i : order) {
-      const uint32_t w = wire_of(i);
-      const bool new_high =
-          w >= 6 && std::find(highs.begin(), highs.end(), w) == highs.end();
-      if (wires.size() == 16 || (new_high && highs.size() == max_high)) flush();
-      if (w >= 6 && std::find(highs.begin(), highs.end(), w) == highs.end()) highs.push_back(w);
-      const PauliString &p = local.terms[i].pauli;
-      wires.push_back(w);
-      signs.push_back(p.y_mask | p.z_mask);
-      nys.push_back(popc(p.y_mask));
-      coeffs.push_back(local.terms[i].coefficient);
-    }
-    flush();
-  }
-  if (!rest.terms.empty()) {
-    for (const FlipGroup &g : group_by_flip(rest)) {
-      for (size_t b = 0; b < g.terms.size(); b += kTermsPerPass) {
-        const uint32_t take =
-            static_cast<uint32_t>(std::min<size_t>(kTermsPerPass, g.terms.size() - b));
-        uint64_t signs[kTermsPerPass];
-        uint32_t nys[kTermsPerPass];
-        double coeffs[kTermsPerPass];
-        for (uint32_t j = 0; j < take; j++) {
-          const PauliTerm &t = rest.terms[g.terms[b + j]];
-          signs[j] = t.pauli.y_mask | t.pauli.z_mask;
-          nys[j] = popc(t.pauli.y_mask);
-          coeffs[j] = t.coefficient;
-        }
-        check(qmk_pauli_accum(costate_, state_, n_, g.flip, take, signs, nys, coeffs,
-                              first ? 1 : 0, stream_),
+  for (const CostateStep &st : costate_schedule(h, n_)) {
+    const uint32_t nt = static_cast<uint32_t>(st.coeffs.size());
+    switch (st.kind) {
+      case CostateStep::ZDiag:
+        check(qmk_zdiag_costate(costate_, state_, n_, nt, st.masks.data(), st.coeffs.data(),
+                                d_results_, ws_, ws_bytes_, stream_),
+              "co-state");
+        dispatches_ += 2;
+        break;
+      case CostateStep::Local:
+        check(qmk_pauli_accum_local(costate_, state_, n_, nt, st.wires.data(), st.masks.data(),
+                                    st.nys.data(), st.coeffs.data(), st.overwrite ? 1 : 0,
+                                    stream_),
               "co-state");
         dispatches_++;
-        first = false;
-      }
+        break;
+      case CostateStep::Flip:
+        check(qmk_pauli_accum(costate_, state_, n_, st.flip, nt, st.masks.data(), st.nys.data(),
+                              st.coeffs.data(), st.overwrite ? 1 : 0, stream_),
+              "co-state");
+        dispatches_++;
+        break;
+      case CostateStep::Zero:
+        cuda_check(cudaMemsetAsync(costate_, 0, dim() * 8, S(stream_)), "co-state zero");
+        break;
+      case CostateStep::Dot:
+        check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
+        dispatches_++;
+        break;
     }
   }
-  if (first) cuda_check(cudaMemsetAsync(costate_, 0, dim() * 8, S(stream_)), "co-state zero");
-  check(qmk_dot_re(state_, costate_, n_, d_results_, ws_, ws_bytes_, stream_), "energy");
-  dispatches_++;
   return 0.0;
 }
 
@@ -1083,227 +838,56 @@ void Simulator::sweep_gate_by_gate(const Circuit &c) {
   }
 }
 
-namespace {
-
-// A run of the circuit that the fused sweep undoes as a unit.
-struct Segment {
-  enum Kind { Window, Diag, Single } kind = Single;
-  size_t begin = 0, end = 0;
-  bool has_param = false;
-  // Diag: the block's forward phase terms and its Z-string generators.
-  std::vector<uint64_t> masks;
-  std::vector<double> angles;
-  double gphase = 0.0;
-  std::vector<uint64_t> gens;
-  std::vector<uint32_t> slots;
-};
-
-// Forward segmentation: a maximal run of one-qubit gates is a window; a run
-// of ZZ couplings (CX.RZ.CX) and two-qubit diagonal gates is a diagonal block;
-// anything else stands alone.
-std::vector<Segment> segment_circuit(const Circuit &c) {
-  std::vector<Segment> segs;
-  const size_t G = c.ops.size();
-  size_t i = 0;
-  while (i < G) {
-    const Gate &g = c.ops[i];
-    Segment s;
-    s.begin = i;
-    uint32_t a, b;
-    double t;
-    if (g.num_qubits == 1) {
-      s.kind = Segment::Window;
-      size_t j = i;
-      for (; j < G && c.ops[j].num_qubits == 1; j++)
-        if (c.ops[j].num_params) s.has_param = true;
-      s.end = j;
-    } else if (zz_coupling_at(c, i, &a, &b, &t) || (g.num_qubits == 2 && is_diagonal(g))) {
-      s.kind = Segment::Diag;
-      size_t j = i;
-      while (j < G) {
-        if (zz_coupling_at(c, j, &a, &b, &t)) {
-          const uint64_t ma = 1ull << a, mb = 1ull << b;
-          s.masks.insert(s.masks.end(), {ma, mb, ma | mb});
-          s.angles.insert(s.angles.end(), {t, t, -2.0 * t});
-          s.gphase += -t / 2.0;
-          if (c.ops[j + 1].num_params) {
-            s.gens.push_back(ma | mb);   // exp(-i t/2 Z_a Z_b)
-            s.slots.push_back(static_cast<uint32_t>(j + 1));
-            s.has_param = true;
-          }
-          j += 3;
-        } else if (c.ops[j].num_qubits == 2 && is_diagonal(c.ops[j])) {
-          s.gphase += diagonal_term(c.ops[j], s.masks, s.angles);
-          if (c.ops[j].num_params) s.has_param = true;
-          j++;
-        } else {
-          break;
-        }
-      }
-      s.end = j;
-    } else {
-      s.kind = Segment::Single;
-      s.end = i + 1;
-      s.has_param = g.num_params > 0;
-    }
-    i = s.end;
-    segs.push_back(std::move(s));
-  }
-  return segs;
-}
-
-struct WireOp {
-  uint32_t wire;
-  float minv[8];
-  int gen;
-  uint32_t slot;
-};
-
-}  // namespace
-
-// Block-wise sweep: every gradient of a commuting block is read at the block
-// boundary and the block is undone on both states in the same pass. Blocks
-// before the first parameterised one are never undone.
+// The block-wise sweep through backward_schedule(): one window-tile pass, one
+// diagonal-block pass or one gather pair per step.
 void Simulator::sweep_fused(const Circuit &c) {
-  const auto segs = segment_circuit(c);
-  size_t first = segs.size();
-  for (size_t s = 0; s < segs.size(); s++)
-    if (segs[s].has_param) {
-      first = s;
-      break;
-    }
-  constexpr uint32_t kOps = 16, kDiagGens = 32;
-  for (size_t s = segs.size(); s-- > first;) {
-    const Segment &seg = segs[s];
-    const bool undo = s > first;
-    if (seg.kind == Segment::Single) {
-      // A run of CX / SWAP gates, all undone here, goes as one permutation
-      // pass per state when that moves fewer bytes.
-      auto perm_gate = [&](size_t k) {
-        const Gate &g = c.ops[segs[k].begin];
-        return segs[k].kind == Segment::Single && (g.kind == G_CX || g.kind == G_SWAP) &&
-               g.qubits[0] < n_ && g.qubits[1] < n_ && g.qubits[0] != g.qubits[1];
-      };
-      if (undo && perm_gate(s)) {
-        size_t lo = s;
-        while (lo - 1 > first && perm_gate(lo - 1)) lo--;
-        if (s > lo) {
-          std::vector<PermGate> run;
-          for (size_t k = lo; k <= s; k++) {
-            const Gate &g = c.ops[segs[k].begin];
-            run.push_back({g.kind == G_SWAP, g.qubits[0], g.qubits[1]});
-          }
-          const Affine map = run_map(n_, run, true);
-          if (permutation_pays(map, run.size()) && permute(state_, map.cols, map.off)) {
-            if (!permute(costate_, map.cols, map.off))
-              throw std::runtime_error("permutation: scratch buffer lost");
-            s = lo;
-            continue;
-          }
-        }
-      }
-      if (undo) {
-        const Gate inv = invert(c.ops[seg.begin]);
-        apply_gate_to(state_, inv);
-        apply_gate_to(costate_, inv);
-      }
-      continue;
-    }
-    if (seg.kind == Segment::Diag) {
-      const uint32_t ng = static_cast<uint32_t>(seg.gens.size());
-      if (ng == 0 && !undo) continue;
-      uint32_t done = 0;
-      do {
-        const uint32_t take = std::min(kDiagGens, ng - done);
-        const bool last = done + take == ng;
-        check(qmk_adjoint_diagonal(state_, costate_, n_, static_cast<uint32_t>(seg.masks.size()),
-                                   seg.masks.data(), seg.angles.data(), seg.gphase, take,
-                                   take ? &seg.gens[done] : nullptr,
-                                   take ? &seg.slots[done] : nullptr, d_grad_,
-                                   (last && undo) ? 1 : 0, ws_, ws_bytes_, stream_),
-              "adjoint diagonal block");
-        dispatches_ += 2;
-        done += take;
-      } while (done < ng);
-      continue;
-    }
-    // Window: each wire's gates last to first, a few wires per pass.
-    std::vector<std::vector<size_t>> per_wire(n_);
-    for (size_t k = seg.begin; k < seg.end; k++) per_wire[c.ops[k].qubits[0]].push_back(k);
-    std::vector<WireOp> tile;
-    uint32_t others = 0, highs = 0, grads = 0;
-    bool tile_has_param = false;
-    const bool wide = n_ >= 6;
-    const uint32_t max_ops = wide ? 32u : kOps;
-    const uint32_t max_high = wide ? std::min<uint32_t>(tile_high_, n_ - 6) : 0;
-    auto flush = [&]() {
-      if (tile.empty()) return;
-      if (undo || tile_has_param) {
+  auto undo_gate = [&](size_t k) {
+    const Gate inv = invert(c.ops[k]);
+    apply_gate_to(state_, inv);
+    apply_gate_to(costate_, inv);
+  };
+  for (const BackwardStep &st : backward_schedule(c, tile_high_)) {
+    switch (st.kind) {
+      case BackwardStep::Window: {
         std::vector<uint32_t> wires, slots;
-        std::vector<float> mats;
+        std::vector<float> mats(8 * st.tile.size());
         std::vector<int> gens;
-        for (const WireOp &o : tile) {
+        for (size_t i = 0; i < st.tile.size(); i++) {
+          const WireOp &o = st.tile[i];
           wires.push_back(o.wire);
-          mats.insert(mats.end(), o.minv, o.minv + 8);
+          narrow(o.minv, &mats[8 * i]);
           gens.push_back(o.gen);
           slots.push_back(o.slot);
         }
-        check(qmk_adjoint_group(state_, costate_, n_, static_cast<uint32_t>(tile.size()),
+        check(qmk_adjoint_group(state_, costate_, n_, static_cast<uint32_t>(st.tile.size()),
                                 wires.data(), mats.data(), gens.data(), slots.data(), d_grad_, ws_,
                                 ws_bytes_, stream_),
               "adjoint window");
         dispatches_++;
+        break;
       }
-      tile.clear();
-      others = highs = grads = 0;
-      tile_has_param = false;
-    };
-    for (uint32_t w = 0; w < n_; w++) {
-      if (per_wire[w].empty()) continue;
-      std::vector<WireOp> ops;
-      uint32_t wgrads = 0;
-      for (size_t r = per_wire[w].size(); r-- > 0;) {
-        const size_t k = per_wire[w][r];
-        const Gate &g = c.ops[k];
-        const Gate inv = invert(g);
-        WireOp o{};
-        o.wire = w;
-        cdouble m[4];
-        gate_matrix_1q(inv.kind, inv.params, m);
-        narrow(m, o.minv);
-        o.gen = g.num_params > 0 ? generator_of(g) : 0;
-        o.slot = static_cast<uint32_t>(k);
-        if (o.gen) wgrads++;
-        ops.push_back(o);
+      case BackwardStep::Diag: {
+        const uint32_t ng = static_cast<uint32_t>(st.gens.size());
+        check(qmk_adjoint_diagonal(state_, costate_, n_, static_cast<uint32_t>(st.masks.size()),
+                                   st.masks.data(), st.angles.data(), st.gphase, ng,
+                                   ng ? st.gens.data() : nullptr, ng ? st.slots.data() : nullptr,
+                                   d_grad_, st.undo ? 1 : 0, ws_, ws_bytes_, stream_),
+              "adjoint diagonal block");
+        dispatches_ += 2;
+        break;
       }
-      const uint32_t need_other = w != 0 ? 1u : 0u, need_high = w >= 6 ? 1u : 0u;
-      if (ops.size() > max_ops || wgrads > 16) {
-        flush();
-        for (size_t b = 0; b < ops.size(); b += kOps) {
-          const size_t e = std::min(ops.size(), b + kOps);
-          tile.assign(ops.begin() + b, ops.begin() + e);
-          for (const WireOp &o : tile) tile_has_param |= o.gen != 0;
-          flush();
+      case BackwardStep::PermuteUndo:
+        if (permute(state_, st.cols, st.off)) {
+          if (!permute(costate_, st.cols, st.off))
+            throw std::runtime_error("permutation: scratch buffer lost");
+        } else {
+          for (size_t k : st.gates) undo_gate(k);
         }
-        continue;
-      }
-      bool full;
-      if (wide) {
-        // Warp tiles: wire 0, wires 1..5 in the lanes, up to four wires >= 6.
-        full = tile.size() + ops.size() > max_ops || highs + need_high > max_high ||
-               grads + wgrads > 16;
-      } else {
-        const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;
-        full = tile.size() + ops.size() > kOps || others + need_other > 3 || grads + wgrads > cap;
-      }
-      if (full) flush();
-      tile.insert(tile.end(), ops.begin(), ops.end());
-      others += need_other;
-      highs += need_high;
-      grads += wgrads;
-      tile_has_param |= wgrads > 0;
+        break;
+      case BackwardStep::GateUndo:
+        undo_gate(st.gates[0]);
+        break;
     }
-    flush();
   }
 }
 
