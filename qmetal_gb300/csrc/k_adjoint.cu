@@ -500,7 +500,7 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
       g.gen[o] = static_cast<int8_t>(gens[o]);
       g.m[o] = m2_from(minv + 8 * o);
       g.cls[o] = m2_class(g.m[o]);
-      g.slotidx[o] = -1;
+      g.slotidx[o] = 0;   // an op without a generator adds zero to slot 0
       if (gens[o]) {
         g.slotidx[o] = static_cast<int8_t>(gi);
         out.slot[gi] = slots[o];

@@ -181,10 +181,13 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
   const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
-  // FP32 per thread over its sites (a few dozen at most), FP64 from the warp up.
-  float accf[NA];
+  // FP32 per thread over its sites (a few dozen at most), FP64 from the warp
+  // up. The per-thread partials live in shared memory, one column per
+  // thread, so an op adds to its slot with one indexed access instead of a
+  // compare-and-add over every register slot.
+  __shared__ float sacc[NA][kThreads];
 #pragma unroll
-  for (int t = 0; t < NA; t++) accf[t] = 0.0f;
+  for (int t = 0; t < NA; t++) sacc[t][threadIdx.x] = 0.0f;
   for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
     uint64_t b = ws;
 #pragma unroll
@@ -210,11 +213,7 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
         case kMatDiag: ov = warp_op<NV, kMatDiag>(P, L, kind, arg, gen, m, lane); break;
         default: ov = warp_op<NV, kMatGeneral>(P, L, kind, arg, gen, m, lane); break;
       }
-      if (NG > 0 && gen) {
-#pragma unroll
-        for (int t = 0; t < NA; t++)
-          if (t == g.slotidx[o]) accf[t] += ov;
-      }
+      if (NG > 0) sacc[g.slotidx[o]][threadIdx.x] += gen ? ov : 0.0f;
     }
 #pragma unroll
     for (int l = 0; l < NV; l++) {
@@ -229,7 +228,7 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   if constexpr (NG > 0) {
     double acc[NA];
 #pragma unroll
-    for (int t = 0; t < NA; t++) acc[t] = accf[t];
+    for (int t = 0; t < NA; t++) acc[t] = sacc[t][threadIdx.x];
     finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
   }
 }
@@ -244,6 +243,14 @@ k_adj_warp(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
 // resident warps to hide the loads and the dependent arithmetic.
 
 constexpr int kPairNV = 8;
+
+// Barrier of the two warps of pair p only (named barrier p + 1; barrier 0 is
+// the block's), so the block's pairs run out of step with each other and
+// one pair's loads overlap another's arithmetic.
+__device__ __forceinline__ void pair_sync(uint32_t p) {
+  asm volatile("bar.sync %0, 64;" ::"r"(p + 1) : "memory");
+}
+static_assert(kThreads / 64 + 1 <= 16, "one named barrier per warp pair");
 
 // The op on the fourth wire for every register vector: own' = s own + t
 // other, own half of the overlap; the partner's vectors come from shared
@@ -297,11 +304,11 @@ k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   float4 *mine_l = xs + (warp * 2 + 1) * NV * 32 + lane;
   const float4 *oth_p = xs + ((warp ^ 1) * 2 + 0) * NV * 32 + lane;
   const float4 *oth_l = xs + ((warp ^ 1) * 2 + 1) * NV * 32 + lane;
-  float accf[NA];
+  __shared__ float sacc[NA][kThreads];   // per-thread FP32 gradient partials
 #pragma unroll
-  for (int t = 0; t < NA; t++) accf[t] = 0.0f;
-  // Every warp of the block runs the same number of rounds (the barriers of
-  // the exchanges must match); a pair past the last tile works on zeros and
+  for (int t = 0; t < NA; t++) sacc[t][tid] = 0.0f;
+  // Both warps of a pair run the same rounds (the barriers of their
+  // exchanges must match); a pair past the last tile works on zeros and
   // stores nothing.
   for (uint64_t r = 0; r < rounds; r++) {
     const uint64_t ws = r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) +
@@ -344,7 +351,7 @@ k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
             mine_p[l * 32] = P[l];
             mine_l[l * 32] = L[l];
           }
-          __syncthreads();
+          pair_sync(warp >> 1);
         }
         const bool one = half != 0;
         switch (cls) {
@@ -353,7 +360,7 @@ k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
           case kMatDiag: ov = split_op<kMatDiag>(P, L, oth_p, oth_l, one, gen, m); break;
           default: ov = split_op<kMatGeneral>(P, L, oth_p, oth_l, one, gen, m); break;
         }
-        if (need) __syncthreads();
+        if (need) pair_sync(warp >> 1);
       } else {
         switch (cls) {
           case kMatReal: ov = warp_op<NV, kMatReal>(P, L, kind, arg, gen, m, lane); break;
@@ -362,11 +369,7 @@ k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
           default: ov = warp_op<NV, kMatGeneral>(P, L, kind, arg, gen, m, lane); break;
         }
       }
-      if (NG > 0 && gen) {
-#pragma unroll
-        for (int t = 0; t < NA; t++)
-          if (t == g.slotidx[o]) accf[t] += ov;
-      }
+      if (NG > 0) sacc[g.slotidx[o]][tid] += gen ? ov : 0.0f;
     }
     if (active) {
 #pragma unroll
@@ -380,7 +383,7 @@ k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   if constexpr (NG > 0) {
     double acc[NA];
 #pragma unroll
-    for (int t = 0; t < NA; t++) acc[t] = accf[t];
+    for (int t = 0; t < NA; t++) acc[t] = sacc[t][tid];
     finish<NG>(acc, static_cast<int>(g.ngrad), a, out);
   }
 }

@@ -124,7 +124,9 @@ struct GroupArgs {
 };
 
 // KP wires >= 1 (plus wire 0 when W0): a site owns 2^KP vectors in registers.
-template <int KP, bool W0>
+// CLS: the structure every matrix of the launch shares (kMat*), so RX-, RY-
+// and phase-like layers take half the multiply-adds of general ones.
+template <int KP, bool W0, int CLS>
 __global__ void __launch_bounds__(kThreads)
 k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
   constexpr int NV = 1 << KP;
@@ -146,7 +148,7 @@ k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
 #pragma unroll
     for (int l = 0; l < NV; l++) {
       float2 x = lo2(r[l]), y = hi2(r[l]);
-      apply2(g.m0, x, y);
+      apply2c(CLS, g.m0, x, y);
       r[l] = pack4(x, y);
     }
   }
@@ -157,8 +159,8 @@ k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
       if ((l >> j) & 1) continue;
       const int h = l | (1 << j);
       float2 a0 = lo2(r[l]), b0 = lo2(r[h]), a1 = hi2(r[l]), b1 = hi2(r[h]);
-      apply2(g.m[j], a0, b0);
-      apply2(g.m[j], a1, b1);
+      apply2c(CLS, g.m[j], a0, b0);
+      apply2c(CLS, g.m[j], a1, b1);
       r[l] = pack4(a0, a1);
       r[h] = pack4(b0, b1);
     }
@@ -187,8 +189,8 @@ struct WarpGroupArgs {
 // wires, so every load and store is a full 512-byte warp access. Wire 0 is a
 // lane-pair update, wires 1..5 exchange with the partner lane by shuffle,
 // wires >= 6 pair registers. Each thread takes UW warp-sites.
-template <int KH, bool W0>
-__global__ void __launch_bounds__(kThreads)
+template <int KH, bool W0, int CLS>
+__global__ void __launch_bounds__(kThreads, 2)
 k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
   constexpr int NV = 1 << KH;
   constexpr int UW = KH <= 1 ? 4 : (KH == 2 ? 2 : 1);
@@ -222,7 +224,7 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         float2 x = lo2(r[u][l]), y = hi2(r[u][l]);
-        apply2(g.m0, x, y);
+        apply2c(CLS, g.m0, x, y);
         r[u][l] = pack4(x, y);
       }
     }
@@ -232,18 +234,19 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
       const uint32_t b = g.lbit[k];
       const bool one = (lane >> b) & 1;
       const M2 m = g.lm[k];
-      const float2 c0 = one ? m.c : m.a, c1 = one ? m.d : m.b;
+      // own' = s own + t other: (a, b) on the wire's 0 side, (d, c) on its 1 side
+      const float2 cs = one ? m.d : m.a, ct = one ? m.c : m.b;
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         const float4 mine = r[u][l];
-        float4 other;
-        other.x = __shfl_xor_sync(0xffffffffu, mine.x, 1 << b);
-        other.y = __shfl_xor_sync(0xffffffffu, mine.y, 1 << b);
-        other.z = __shfl_xor_sync(0xffffffffu, mine.z, 1 << b);
-        other.w = __shfl_xor_sync(0xffffffffu, mine.w, 1 << b);
-        const float4 zero_side = one ? other : mine, one_side = one ? mine : other;
-        r[u][l] = pack4(cmac2(c0, lo2(zero_side), c1, lo2(one_side)),
-                        cmac2(c0, hi2(zero_side), c1, hi2(one_side)));
+        if (CLS == kMatDiag) {
+          r[u][l] = pack4(cmac2c(CLS, cs, lo2(mine), ct, lo2(mine)),
+                          cmac2c(CLS, cs, hi2(mine), ct, hi2(mine)));
+        } else {
+          const float4 other = shfl4(mine, 1 << b);
+          r[u][l] = pack4(cmac2c(CLS, cs, lo2(mine), ct, lo2(other)),
+                          cmac2c(CLS, cs, hi2(mine), ct, hi2(other)));
+        }
       }
     }
 #pragma unroll
@@ -253,8 +256,8 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
         if ((l >> j) & 1) continue;
         const int h = l | (1 << j);
         float2 a0 = lo2(r[u][l]), b0 = lo2(r[u][h]), a1 = hi2(r[u][l]), b1 = hi2(r[u][h]);
-        apply2(g.hm[j], a0, b0);
-        apply2(g.hm[j], a1, b1);
+        apply2c(CLS, g.hm[j], a0, b0);
+        apply2c(CLS, g.hm[j], a1, b1);
         r[u][l] = pack4(a0, a1);
         r[u][h] = pack4(b0, b1);
       }
@@ -530,10 +533,39 @@ extern "C" int qmk_apply_phase(float *state, uint32_t n, uint64_t mask,
   return launch_status();
 }
 
+// The narrowest kMat* structure all k matrices share (kMatGeneral if none).
+static int8_t common_class(const M2 *ms, int k) {
+  bool diag = true, rx = true, real = true;
+  for (int j = 0; j < k; j++) {
+    const M2 &m = ms[j];
+    diag &= m.b.x == 0.0f && m.b.y == 0.0f && m.c.x == 0.0f && m.c.y == 0.0f;
+    rx &= m.a.y == 0.0f && m.d.y == 0.0f && m.b.x == 0.0f && m.c.x == 0.0f;
+    real &= m.a.y == 0.0f && m.b.y == 0.0f && m.c.y == 0.0f && m.d.y == 0.0f;
+  }
+  return diag ? kMatDiag : (rx ? kMatRx : (real ? kMatReal : kMatGeneral));
+}
+
 template <int KP, bool W0>
-static void launch_group(float4 *st, uint64_t nsites, const GroupArgs &g,
+static void launch_group(float4 *st, uint64_t nsites, const GroupArgs &g, int cls,
                          cudaStream_t stream) {
-  k_group<KP, W0><<<grid_for(nsites, kThreads), kThreads, 0, stream>>>(st, nsites, g);
+  const unsigned grid = grid_for(nsites, kThreads);
+  switch (cls) {
+    case kMatDiag: k_group<KP, W0, kMatDiag><<<grid, kThreads, 0, stream>>>(st, nsites, g); break;
+    case kMatRx: k_group<KP, W0, kMatRx><<<grid, kThreads, 0, stream>>>(st, nsites, g); break;
+    case kMatReal: k_group<KP, W0, kMatReal><<<grid, kThreads, 0, stream>>>(st, nsites, g); break;
+    default: k_group<KP, W0, kMatGeneral><<<grid, kThreads, 0, stream>>>(st, nsites, g); break;
+  }
+}
+
+template <int KH, bool W0>
+static void launch_group_warp(float4 *st, uint64_t nw, const WarpGroupArgs &g, int cls,
+                              unsigned grid, cudaStream_t s) {
+  switch (cls) {
+    case kMatDiag: k_group_warp<KH, W0, kMatDiag><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+    case kMatRx: k_group_warp<KH, W0, kMatRx><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+    case kMatReal: k_group_warp<KH, W0, kMatReal><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+    default: k_group_warp<KH, W0, kMatGeneral><<<grid, kThreads, 0, s>>>(st, nw, g); break;
+  }
 }
 
 extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
@@ -571,17 +603,20 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
       const uint64_t nw = 1ull << (n - 6 - kh);
       const int uw = kh <= 1 ? 4 : (kh == 2 ? 2 : 1);
       const unsigned grid = grid_for(nw, (kThreads / 32) * uw);
+      std::vector<M2> all;
+      for (uint32_t j = 0; j < k; j++) all.push_back(m2_from(mats + 8 * j));
+      const int cls = common_class(all.data(), static_cast<int>(k));
       switch (kh * 2 + (w0 ? 1 : 0)) {
-        case 0: k_group_warp<0, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 1: k_group_warp<0, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 2: k_group_warp<1, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 3: k_group_warp<1, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 4: k_group_warp<2, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 5: k_group_warp<2, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 6: k_group_warp<3, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 7: k_group_warp<3, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 8: k_group_warp<4, false><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
-        case 9: k_group_warp<4, true><<<grid, kThreads, 0, s>>>(st, nw, wg); break;
+        case 0: launch_group_warp<0, false>(st, nw, wg, cls, grid, s); break;
+        case 1: launch_group_warp<0, true>(st, nw, wg, cls, grid, s); break;
+        case 2: launch_group_warp<1, false>(st, nw, wg, cls, grid, s); break;
+        case 3: launch_group_warp<1, true>(st, nw, wg, cls, grid, s); break;
+        case 4: launch_group_warp<2, false>(st, nw, wg, cls, grid, s); break;
+        case 5: launch_group_warp<2, true>(st, nw, wg, cls, grid, s); break;
+        case 6: launch_group_warp<3, false>(st, nw, wg, cls, grid, s); break;
+        case 7: launch_group_warp<3, true>(st, nw, wg, cls, grid, s); break;
+        case 8: launch_group_warp<4, false>(st, nw, wg, cls, grid, s); break;
+        case 9: launch_group_warp<4, true>(st, nw, wg, cls, grid, s); break;
         default: return -1;
       }
       return launch_status();
@@ -601,18 +636,21 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
   }
   if (static_cast<uint32_t>(kp) > n - 1) return -1;
   const uint64_t nsites = 1ull << (n - 1 - kp);
+  std::vector<M2> all;
+  for (uint32_t j = 0; j < k; j++) all.push_back(m2_from(mats + 8 * j));
+  const int cls = common_class(all.data(), static_cast<int>(k));
   switch (kp * 2 + (w0 ? 1 : 0)) {
-    case 1: launch_group<0, true>(st, nsites, g, s); break;
-    case 2: launch_group<1, false>(st, nsites, g, s); break;
-    case 3: launch_group<1, true>(st, nsites, g, s); break;
-    case 4: launch_group<2, false>(st, nsites, g, s); break;
-    case 5: launch_group<2, true>(st, nsites, g, s); break;
-    case 6: launch_group<3, false>(st, nsites, g, s); break;
-    case 7: launch_group<3, true>(st, nsites, g, s); break;
-    case 8: launch_group<4, false>(st, nsites, g, s); break;
-    case 9: launch_group<4, true>(st, nsites, g, s); break;
-    case 10: launch_group<5, false>(st, nsites, g, s); break;
-    case 11: launch_group<5, true>(st, nsites, g, s); break;
+    case 1: launch_group<0, true>(st, nsites, g, cls, s); break;
+    case 2: launch_group<1, false>(st, nsites, g, cls, s); break;
+    case 3: launch_group<1, true>(st, nsites, g, cls, s); break;
+    case 4: launch_group<2, false>(st, nsites, g, cls, s); break;
+    case 5: launch_group<2, true>(st, nsites, g, cls, s); break;
+    case 6: launch_group<3, false>(st, nsites, g, cls, s); break;
+    case 7: launch_group<3, true>(st, nsites, g, cls, s); break;
+    case 8: launch_group<4, false>(st, nsites, g, cls, s); break;
+    case 9: launch_group<4, true>(st, nsites, g, cls, s); break;
+    case 10: launch_group<5, false>(st, nsites, g, cls, s); break;
+    case 11: launch_group<5, true>(st, nsites, g, cls, s); break;
     default: return -1;
   }
   return launch_status();

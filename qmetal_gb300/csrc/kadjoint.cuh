@@ -21,7 +21,7 @@ struct WarpAdjArgs {
                                  // 3: the wire split across a warp pair
   int8_t arg[kMaxWarpOps];       // lane bit (0..4) or register index
   int8_t gen[kMaxWarpOps];
-  int8_t slotidx[kMaxWarpOps];
+  int8_t slotidx[kMaxWarpOps];   // gradient slot of op o (0 when gen[o] is 0)
   int8_t cls[kMaxWarpOps];       // kMat* structure of m
   M2 m[kMaxWarpOps];
 };
