@@ -135,6 +135,9 @@ k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
   uint64_t base = s;
 #pragma unroll
   for (int j = 0; j < KP; j++) base = ins0(base, g.pos[j]);
+  // Scalar arithmetic: at up to 32 vectors a thread this kernel is bound by
+  // its one block per SM, and the packed form's extra registers cost more
+  // than its saved instructions.
   float4 r[NV];
 #pragma unroll
   for (int l = 0; l < NV; l++) {
@@ -180,7 +183,7 @@ struct WarpGroupArgs {
   uint32_t lbit[5];  // their vector bits (0..4)
   M2 lm[5];
   uint32_t hpos[4];  // wires >= 6: vector bits - 5 (warp-site bits), ascending
-  M2 hm[4];
+  MX hm[4];
   M2 m0;             // wire 0 (lanes) when W0
 };
 
@@ -197,7 +200,7 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t warp = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
   uint64_t base[UW];
-  float4 r[UW][NV];
+  Cx2 r[UW][NV];
 #pragma unroll
   for (int u = 0; u < UW; u++) {
     const uint64_t ws = warp * UW + u;
@@ -213,7 +216,7 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
 #pragma unroll
       for (int j = 0; j < KH; j++)
         if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
-      r[u][l] = st[v];
+      r[u][l] = split2(st[v]);
     }
   }
 #pragma unroll
@@ -222,15 +225,11 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
     if (base[u] == ~0ull) continue;
     if (W0) {
 #pragma unroll
-      for (int l = 0; l < NV; l++) {
-        float2 x = lo2(r[u][l]), y = hi2(r[u][l]);
-        apply2c(CLS, g.m0, x, y);
-        r[u][l] = pack4(x, y);
-      }
+      for (int l = 0; l < NV; l++) apply_w0x<CLS>(g.m0, r[u][l]);
     }
 #pragma unroll
     for (int k = 0; k < 5; k++) {
-      if (k >= static_cast<int>(g.nlow)) break;
+      if (k >= static_cast<int>(g.nlow)) continue;   // (a break here spills)
       const uint32_t b = g.lbit[k];
       const bool one = (lane >> b) & 1;
       const M2 m = g.lm[k];
@@ -238,14 +237,16 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
       const float2 cs = one ? m.d : m.a, ct = one ? m.c : m.b;
 #pragma unroll
       for (int l = 0; l < NV; l++) {
-        const float4 mine = r[u][l];
         if (CLS == kMatDiag) {
-          r[u][l] = pack4(cmac2c(CLS, cs, lo2(mine), ct, lo2(mine)),
-                          cmac2c(CLS, cs, hi2(mine), ct, hi2(mine)));
+          r[u][l] = cmacx<CLS>(cs, r[u][l], ct, r[u][l]);
         } else {
-          const float4 other = shfl4(mine, 1 << b);
-          r[u][l] = pack4(cmac2c(CLS, cs, lo2(mine), ct, lo2(other)),
-                          cmac2c(CLS, cs, hi2(mine), ct, hi2(other)));
+          const Cx2 mine = r[u][l];
+          Cx2 other;
+          other.re.x = __shfl_xor_sync(0xffffffffu, mine.re.x, 1 << b);
+          other.re.y = __shfl_xor_sync(0xffffffffu, mine.re.y, 1 << b);
+          other.im.x = __shfl_xor_sync(0xffffffffu, mine.im.x, 1 << b);
+          other.im.y = __shfl_xor_sync(0xffffffffu, mine.im.y, 1 << b);
+          r[u][l] = cmacx<CLS>(cs, mine, ct, other);
         }
       }
     }
@@ -254,12 +255,7 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         if ((l >> j) & 1) continue;
-        const int h = l | (1 << j);
-        float2 a0 = lo2(r[u][l]), b0 = lo2(r[u][h]), a1 = hi2(r[u][l]), b1 = hi2(r[u][h]);
-        apply2c(CLS, g.hm[j], a0, b0);
-        apply2c(CLS, g.hm[j], a1, b1);
-        r[u][l] = pack4(a0, a1);
-        r[u][h] = pack4(b0, b1);
+        applyx<CLS>(g.hm[j], r[u][l], r[u][l | (1 << j)]);
       }
     }
 #pragma unroll
@@ -268,7 +264,7 @@ k_group_warp(float4 *__restrict__ st, uint64_t nwsites, WarpGroupArgs g) {
 #pragma unroll
       for (int j = 0; j < KH; j++)
         if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
-      st[v] = r[u][l];
+      st[v] = join2(r[u][l]);
     }
   }
 }
@@ -595,7 +591,7 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
       } else {
         if (kh == 4) { kh = -1; break; }
         wg.hpos[kh] = q - 6;
-        wg.hm[kh] = m2_from(mats + 8 * j);
+        wg.hm[kh] = mx_from(m2_from(mats + 8 * j));
         kh++;
       }
     }

@@ -86,6 +86,80 @@ __device__ __forceinline__ float4 pack4(float2 a, float2 b) {
   return make_float4(a.x, a.y, b.x, b.y);
 }
 
+// The two amplitudes of one vector held as (re0, re1) and (im0, im1): an op
+// on any wire but 0 updates both amplitudes with the same coefficients, so
+// each real multiply-add runs as one packed FP32x2 instruction (sm_100 and
+// later) instead of two.
+struct Cx2 {
+  float2 re, im;
+};
+__device__ __forceinline__ Cx2 split2(const float4 &v) {
+  return {make_float2(v.x, v.z), make_float2(v.y, v.w)};
+}
+__device__ __forceinline__ float4 join2(const Cx2 &c) {
+  return make_float4(c.re.x, c.im.x, c.re.y, c.im.y);
+}
+__device__ __forceinline__ float2 bc2(float x) { return make_float2(x, x); }
+
+// s * own + t * other for both amplitudes, s and t of a class-cls matrix
+// (the packed counterpart of cmac2c), from their parts as broadcast pairs:
+// sr = (s.x, s.x), si = (s.y, s.y), nsi = -si, and the same for t.
+template <int CLS>
+__device__ __forceinline__ Cx2 cmacx6(float2 sr, float2 si, float2 nsi, float2 tr, float2 ti,
+                                      float2 nti, const Cx2 &own, const Cx2 &oth) {
+  Cx2 r;
+  if (CLS == kMatReal) {
+    r.re = __ffma2_rn(tr, oth.re, __fmul2_rn(sr, own.re));
+    r.im = __ffma2_rn(tr, oth.im, __fmul2_rn(sr, own.im));
+  } else if (CLS == kMatRx) {
+    r.re = __ffma2_rn(nti, oth.im, __fmul2_rn(sr, own.re));
+    r.im = __ffma2_rn(ti, oth.re, __fmul2_rn(sr, own.im));
+  } else if (CLS == kMatDiag) {
+    r.re = __ffma2_rn(nsi, own.im, __fmul2_rn(sr, own.re));
+    r.im = __ffma2_rn(si, own.re, __fmul2_rn(sr, own.im));
+  } else {
+    r.re = __ffma2_rn(nti, oth.im,
+                      __ffma2_rn(tr, oth.re, __ffma2_rn(nsi, own.im, __fmul2_rn(sr, own.re))));
+    r.im = __ffma2_rn(ti, oth.re,
+                      __ffma2_rn(tr, oth.im, __ffma2_rn(si, own.re, __fmul2_rn(sr, own.im))));
+  }
+  return r;
+}
+
+template <int CLS>
+__device__ __forceinline__ Cx2 cmacx(float2 s, const Cx2 &own, float2 t, const Cx2 &oth) {
+  return cmacx6<CLS>(bc2(s.x), bc2(s.y), bc2(-s.y), bc2(t.x), bc2(t.y), bc2(-t.y), own, oth);
+}
+
+// A 2x2 with its parts pre-broadcast to pairs (imaginary parts also
+// negated): the operands of the packed updates, built once on the host.
+struct MX {
+  float2 ar, ai, nai, br, bi, nbi, cr, ci, nci, dr, di, ndi;
+};
+__host__ inline MX mx_from(const M2 &m) {
+  auto b = [](float x) { return make_float2(x, x); };
+  return {b(m.a.x), b(m.a.y), b(-m.a.y), b(m.b.x), b(m.b.y), b(-m.b.y),
+          b(m.c.x), b(m.c.y), b(-m.c.y), b(m.d.x), b(m.d.y), b(-m.d.y)};
+}
+
+// (u, v) <- m (u, v) for a pair of vectors across one wire >= 1.
+template <int CLS>
+__device__ __forceinline__ void applyx(const MX &m, Cx2 &u, Cx2 &v) {
+  const Cx2 nu = cmacx6<CLS>(m.ar, m.ai, m.nai, m.br, m.bi, m.nbi, u, v);
+  const Cx2 nv = cmacx6<CLS>(m.dr, m.di, m.ndi, m.cr, m.ci, m.nci, v, u);
+  u = nu;
+  v = nv;
+}
+
+// m on wire 0: the two amplitudes of one vector are the pair.
+template <int CLS>
+__device__ __forceinline__ void apply_w0x(const M2 &m, Cx2 &x) {
+  float2 u = make_float2(x.re.x, x.im.x), v = make_float2(x.re.y, x.im.y);
+  apply2c(CLS, m, u, v);
+  x.re = make_float2(u.x, v.x);
+  x.im = make_float2(u.y, v.y);
+}
+
 // Insert a zero bit at position p (bits >= p move up one).
 __device__ __forceinline__ uint64_t ins0(uint64_t x, uint32_t p) {
   const uint64_t low = x & ((1ull << p) - 1ull);
