@@ -178,10 +178,13 @@ int qmk_adjoint_diagonal(float *psi, float *lambda, uint32_t n, uint32_t num_ter
                          double *d_grad, int undo, void *workspace, size_t workspace_bytes,
                          void *stream);
 
-/* Backward step over one-qubit gates on at most three wires >= 1 plus wire 0,
- * applied in the given order (each wire's gates last to first): op o takes
- * d_grad[slots[o]] = Im<lambda|P|psi> if gens[o] is 1/2/3 (X/Y/Z), then
- * applies minv[8o..8o+7] to both states; up to 16 ops, one pass. Replaces the
+/* Backward step over a window tile of one-qubit gates, applied in the given
+ * order (each wire's gates last to first): op o takes d_grad[slots[o]] =
+ * Im<lambda|P|psi> if gens[o] is 1/2/3 (X/Y/Z), then applies
+ * minv[8o..8o+7] to both states; one pass. From n >= 6 + h a tile holds wire
+ * 0, any of wires 1..5 and h <= 4 wires >= 6, up to 32 ops of which up to 16
+ * carry a gradient; below that, wire 0 and up to three wires >= 1 and 16
+ * ops. Returns -1 (nothing launched) for any other shape. Replaces the
  * per-gate reduce_pauli2 and undo dispatches (kernels.metal:331-360;
  * simulator.mm:914-959). */
 int qmk_adjoint_group(float *psi, float *lambda, uint32_t n, uint32_t num_ops,
