@@ -388,6 +388,189 @@ k_adj_pair(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Uniform warp-pair tiles: one rotation per wire, every op of the same kind
+// (all RX, all RY or all RZ), on wire 0 and all five lane wires or on the
+// four register wires alone -- the mixer and rotation layers of QAOA, TFIM
+// and hardware-efficient circuits. The op list is then known at compile
+// time: no per-op dispatch, gradient partials in registers at fixed
+// indices, and the compiler free to interleave one op's shuffles with
+// another's arithmetic. Same per-op arithmetic and order as k_adj_pair.
+
+struct UniArgs {
+  uint32_t hpos[4];   // wires >= 6: vector bit - 5, ascending; hpos[3] is split
+  uint32_t lbit[5];   // lane wires' vector bits
+  M2 m0, ml[5], mh[4];
+};
+
+template <bool W0, int NL, int CLS, int GEN>
+__global__ void __launch_bounds__(kThreads, 2)
+k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, UniArgs g,
+               Area a, OutSlots<(W0 ? 1 : 0) + NL + 4> out) {
+  constexpr int NV = kPairNV;
+  constexpr int NOPS = (W0 ? 1 : 0) + NL + 4;
+  constexpr int LANE0 = W0 ? 1 : 0, REG0 = LANE0 + NL;
+  extern __shared__ __align__(16) float4 xs[];   // [warp][state][NV][32 lanes]
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t half = warp & 1;
+  const uint64_t per_round = static_cast<uint64_t>(gridDim.x) * (kThreads / 64);
+  const uint64_t rounds = (nwsites + per_round - 1) / per_round;
+  float4 *mine_p = xs + (warp * 2 + 0) * NV * 32 + lane;
+  float4 *mine_l = xs + (warp * 2 + 1) * NV * 32 + lane;
+  const float4 *oth_p = xs + ((warp ^ 1) * 2 + 0) * NV * 32 + lane;
+  const float4 *oth_l = xs + ((warp ^ 1) * 2 + 1) * NV * 32 + lane;
+  float accf[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
+  for (uint64_t r = 0; r < rounds; r++) {
+    const uint64_t ws = r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) +
+                        (warp >> 1);
+    const bool active = ws < nwsites;
+    uint64_t base = 0;
+    if (active) {
+      uint64_t b = ws;
+#pragma unroll
+      for (int j = 0; j < 4; j++) b = ins0(b, g.hpos[j]);
+      base = (b << 5) | lane | (static_cast<uint64_t>(half) << (g.hpos[3] + 5));
+    }
+    auto vec_of = [&](int l) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      return v;
+    };
+    float4 P[NV], L[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      if (active) {
+        const uint64_t v = vec_of(l);
+        P[l] = psi[v];
+        L[l] = lam[v];
+      } else {
+        P[l] = L[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    if (W0) accf[0] += wire0_op<NV, CLS>(P, L, GEN, g.m0);
+#pragma unroll
+    for (int k = 0; k < NL; k++)
+      accf[LANE0 + k] += lane_op_g<NV, CLS, GEN>(P, L, 1 << g.lbit[k], (lane >> g.lbit[k]) & 1,
+                                                 g.ml[k]);
+    accf[REG0 + 0] += reg_op<NV, 0, CLS>(P, L, GEN, g.mh[0]);
+    accf[REG0 + 1] += reg_op<NV, 1, CLS>(P, L, GEN, g.mh[1]);
+    accf[REG0 + 2] += reg_op<NV, 2, CLS>(P, L, GEN, g.mh[2]);
+    constexpr bool kNeed = CLS != kMatDiag || GEN == 1 || GEN == 2;
+    if (kNeed) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        mine_p[l * 32] = P[l];
+        mine_l[l * 32] = L[l];
+      }
+      pair_sync(warp >> 1);
+    }
+    accf[REG0 + 3] += split_op_g<CLS, GEN>(P, L, oth_p, oth_l, half != 0, g.mh[3]);
+    if (kNeed) pair_sync(warp >> 1);
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        const uint64_t v = vec_of(l);
+        psi[v] = P[l];
+        lam[v] = L[l];
+      }
+    }
+  }
+  double acc[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) acc[t] = accf[t];
+  finish<NOPS>(acc, NOPS, a, out);
+}
+
+template <bool W0, int NL, int CLS, int GEN>
+int launch_adj_pair_uni(float4 *psi, float4 *lam, uint64_t nwsites, const UniArgs &g,
+                        double *grad, const uint32_t *slots, Area a, cudaStream_t s) {
+  constexpr int NOPS = (W0 ? 1 : 0) + NL + 4;
+  OutSlots<NOPS> out{};
+  out.p = grad;
+  for (int t = 0; t < NOPS; t++) out.slot[t] = slots[t];
+  unsigned grid = grid_for(nwsites, kThreads / 64);
+  grid = std::min<unsigned>(grid, reduce_grid());
+  const size_t smem = static_cast<size_t>(kThreads / 32) * 2 * kPairNV * 32 * sizeof(float4);
+  static bool opted[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (!opted[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(k_adj_pair_uni<W0, NL, CLS, GEN>,
+                                               cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    opted[dev] = true;
+  }
+  k_adj_pair_uni<W0, NL, CLS, GEN><<<grid, kThreads, smem, s>>>(psi, lam, nwsites, g, a, out);
+  return launch_status();
+}
+
+// A four-register-wire tile with one rotation per wire, all RX (class RX,
+// generator X), all RY (real, Y) or all RZ (diagonal, Z), on the four
+// register wires alone or with wire 0 and all five lane wires, goes to the
+// uniform kernel. Returns 1 (nothing launched) for any other tile.
+int launch_uniform(float4 *psi, float4 *lam, uint64_t nw, const WarpAdjArgs &g,
+                   const OutSlots<kMaxGen> &out, Area a, cudaStream_t s) {
+  if (g.nops != 4 && g.nops != 10) return 1;
+  const int cls = g.cls[0], gen = g.gen[0];
+  if (!((cls == kMatRx && gen == 1) || (cls == kMatReal && gen == 2) ||
+        (cls == kMatDiag && gen == 3)))
+    return 1;
+  UniArgs u{};
+  for (int j = 0; j < 4; j++) u.hpos[j] = g.hpos[j];
+  int w0 = 0, nl = 0;
+  bool seen_h[4] = {false, false, false, false};
+  uint32_t lanes_seen = 0, slot_w0 = 0, slot_l[5] = {}, slot_h[4] = {};
+  for (uint32_t o = 0; o < g.nops; o++) {
+    if (g.cls[o] != cls || g.gen[o] != gen) return 1;
+    const uint32_t slot = out.slot[g.slotidx[o]];
+    if (g.kind[o] == 0) {
+      if (w0) return 1;
+      w0 = 1;
+      u.m0 = g.m[o];
+      slot_w0 = slot;
+    } else if (g.kind[o] == 1) {
+      const int b = g.arg[o];
+      if (b < 0 || b > 4 || ((lanes_seen >> b) & 1u)) return 1;
+      lanes_seen |= 1u << b;
+      u.lbit[nl] = static_cast<uint32_t>(b);
+      u.ml[nl] = g.m[o];
+      slot_l[nl] = slot;
+      nl++;
+    } else if (g.kind[o] == 2) {
+      const int j = g.arg[o];
+      if (j < 0 || j > 3 || seen_h[j]) return 1;
+      seen_h[j] = true;
+      u.mh[j] = g.m[o];
+      slot_h[j] = slot;
+    } else {
+      return 1;
+    }
+  }
+  for (int j = 0; j < 4; j++)
+    if (!seen_h[j]) return 1;
+  const bool wide = w0 == 1 && nl == 5;
+  if (!wide && !(w0 == 0 && nl == 0)) return 1;
+  uint32_t slots[10];
+  int t = 0;
+  if (w0) slots[t++] = slot_w0;
+  for (int k = 0; k < nl; k++) slots[t++] = slot_l[k];
+  for (int j = 0; j < 4; j++) slots[t++] = slot_h[j];
+  double *p = out.p;
+  if (wide) {
+    if (gen == 1) return launch_adj_pair_uni<true, 5, kMatRx, 1>(psi, lam, nw, u, p, slots, a, s);
+    if (gen == 2) return launch_adj_pair_uni<true, 5, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+    return launch_adj_pair_uni<true, 5, kMatDiag, 3>(psi, lam, nw, u, p, slots, a, s);
+  }
+  if (gen == 1) return launch_adj_pair_uni<false, 0, kMatRx, 1>(psi, lam, nw, u, p, slots, a, s);
+  if (gen == 2) return launch_adj_pair_uni<false, 0, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+  return launch_adj_pair_uni<false, 0, kMatDiag, 3>(psi, lam, nw, u, p, slots, a, s);
+}
+
 template <int NG>
 int launch_adj_pair(float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArgs &g,
                     const OutSlots<kMaxGen> &slots, Area a, cudaStream_t s) {
@@ -429,6 +612,8 @@ void launch_adj_warp(float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjAr
 int launch_tiles(int kh, int ng, float4 *psi, float4 *lam, uint64_t nw, WarpAdjArgs &g,
                  const OutSlots<kMaxGen> &out, Area a, cudaStream_t s) {
   if (kh == 4) {
+    const int rc = launch_uniform(psi, lam, nw, g, out, a, s);
+    if (rc != 1) return rc;
     // two warps per tile: the fourth register wire is split across the pair
     for (uint32_t o = 0; o < g.nops; o++)
       if (g.kind[o] == 2 && g.arg[o] == 3) g.kind[o] = 3;

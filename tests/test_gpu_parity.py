@@ -461,6 +461,32 @@ def test_fused_adjoint_tiles_and_lanes(n):
     assert np.abs(np.array(g1) - g0).max() <= 1e-5
 
 
+@pytest.mark.parametrize("n", [10, 14])
+def test_uniform_rotation_layers(n):
+    """Layers of one rotation kind on every wire (RX, RY, RZ) take the
+    compile-time-uniform window tiles (wire 0 + wires 1..5 + four wires >= 6,
+    and four wires >= 6 alone); zero angles and a mixed layer take the
+    general tiles. Both sweeps against the oracle's adjoint."""
+    rng = np.random.default_rng(900 + n)
+    ang = lambda: float(rng.uniform(-3, 3))
+    gates = [(H, (q,), ()) for q in range(n)]
+    entangle = [(CX, (q, q + 1), ()) for q in range(0, n - 1, 2)]
+    entangle += [(CZ, (q, q + 1), ()) for q in range(1, n - 1, 2)]
+    for kind in (RX, RY, RZ):
+        gates += entangle + [(kind, (q,), (ang(),)) for q in range(n)]
+    gates += entangle + [(RX, (q,), (0.0,)) for q in range(n)]             # rotations by zero
+    gates += entangle + [((RY if q == 7 else RX), (q,), (ang(),)) for q in range(n)]
+    terms = W.ring_tfim_hamiltonian(n, 0.7) + [(0.4, 1 << 3, 1 << 8, 0)]
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    c, h = W.to_circuit(n, gates), W.to_hamiltonian(terms)
+    sim = qm.Simulator(n)
+    e1, g1 = sim.energy_and_gradient(c, h)
+    e2, g2 = sim.energy_and_gradient(c, h, fused=False)
+    assert abs(e1 - e0) <= 1e-5 and abs(e2 - e0) <= 1e-5
+    assert np.abs(np.array(g1) - g0).max() <= 1e-5
+    assert np.abs(np.array(g2) - g0).max() <= 1e-5
+
+
 def test_gradient_matches_oracle_adjoint_wide():
     """All gate kinds in the backward sweep, every wire, n = 12."""
     n = 12
