@@ -1,0 +1,362 @@
+// k_adjoint_uniform.cu -- window tiles whose op list is fixed at compile
+// time: every wire of the tile carries the same short sequence of rotations
+// (one RX, RY or RZ per wire -- the mixer and rotation layers of QAOA and
+// TFIM circuits -- or RZ then RY, the backward order of a hardware-efficient
+// layer). With the sequence known there is no per-op dispatch, the gradient
+// partials sit in registers at fixed indices, and the compiler may interleave
+// one op's shuffles with another's arithmetic. The per-op arithmetic and the
+// op order are those of the general tiles (k_adjoint_tiles.cu), so results
+// are the same bits.
+#include <algorithm>
+
+#include "kadjoint_ops.cuh"
+
+using namespace qmk;
+using qmk_host::grid_for;
+using qmk_host::launch_status;
+
+namespace qmk_adj {
+namespace {
+
+// Matrices of a uniform tile: op k of wire 0, of lane wire i, of register
+// wire j.
+struct UniArgs {
+  uint32_t hpos[4];   // wires >= 6: vector bit - 5, ascending
+  uint32_t lbit[5];   // lane wires' vector bits, in op order
+  M2 m0[2], ml[5][2], mh[4][2];
+};
+
+// The M ops of one wire: op k has class Ck and generator Gk.
+template <int M, int NV, int C0, int G0, int C1, int G1>
+__device__ __forceinline__ void w0_ops(float4 (&P)[NV], float4 (&L)[NV], const M2 (&m)[2],
+                                       float *acc) {
+  acc[0] += wire0_op<NV, C0>(P, L, G0, m[0]);
+  if constexpr (M > 1) acc[1] += wire0_op<NV, C1>(P, L, G1, m[1]);
+}
+template <int M, int NV, int C0, int G0, int C1, int G1>
+__device__ __forceinline__ void lane_ops(float4 (&P)[NV], float4 (&L)[NV], uint32_t bit,
+                                         uint32_t lane, const M2 (&m)[2], float *acc) {
+  const int mask = 1 << bit;
+  const bool one = (lane >> bit) & 1;
+  acc[0] += lane_op_g<NV, C0, G0>(P, L, mask, one, m[0]);
+  if constexpr (M > 1) acc[1] += lane_op_g<NV, C1, G1>(P, L, mask, one, m[1]);
+}
+template <int M, int NV, int J, int C0, int G0, int C1, int G1>
+__device__ __forceinline__ void reg_ops(float4 (&P)[NV], float4 (&L)[NV], const M2 (&m)[2],
+                                        float *acc) {
+  acc[0] += reg_op<NV, J, C0>(P, L, G0, m[0]);
+  if constexpr (M > 1) acc[1] += reg_op<NV, J, C1>(P, L, G1, m[1]);
+}
+
+// One op on the wire split across a warp pair: the pair trades vectors
+// through shared memory unless the op is diagonal with a Z (or no)
+// generator.
+template <int C, int G>
+__device__ __forceinline__ float split_one(float4 (&P)[kPairNV], float4 (&L)[kPairNV],
+                                           float4 *mine_p, float4 *mine_l, const float4 *oth_p,
+                                           const float4 *oth_l, bool one, uint32_t pair,
+                                           const M2 &m) {
+  constexpr bool kNeed = C != kMatDiag || G == 1 || G == 2;
+  if (kNeed) {
+#pragma unroll
+    for (int l = 0; l < kPairNV; l++) {
+      mine_p[l * 32] = P[l];
+      mine_l[l * 32] = L[l];
+    }
+    pair_sync(pair);
+  }
+  const float ov = split_op_g<C, G>(P, L, oth_p, oth_l, one, m);
+  if (kNeed) pair_sync(pair);
+  return ov;
+}
+
+// Four register wires on a warp pair (the fourth split across the pair),
+// optionally with wire 0 and the five lane wires.
+template <bool W0, int NL, int M, int C0, int G0, int C1, int G1>
+__global__ void __launch_bounds__(kThreads, 2)
+k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, UniArgs g,
+               Area a, OutSlots<M *((W0 ? 1 : 0) + NL + 4)> out) {
+  constexpr int NV = kPairNV;
+  constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + 4);
+  constexpr int LANE0 = M * (W0 ? 1 : 0), REG0 = LANE0 + M * NL;
+  extern __shared__ __align__(16) float4 xs[];   // [warp][state][NV][32 lanes]
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t half = warp & 1;
+  const uint64_t per_round = static_cast<uint64_t>(gridDim.x) * (kThreads / 64);
+  const uint64_t rounds = (nwsites + per_round - 1) / per_round;
+  float4 *mine_p = xs + (warp * 2 + 0) * NV * 32 + lane;
+  float4 *mine_l = xs + (warp * 2 + 1) * NV * 32 + lane;
+  const float4 *oth_p = xs + ((warp ^ 1) * 2 + 0) * NV * 32 + lane;
+  const float4 *oth_l = xs + ((warp ^ 1) * 2 + 1) * NV * 32 + lane;
+  float accf[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
+  for (uint64_t r = 0; r < rounds; r++) {
+    const uint64_t ws = r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) +
+                        (warp >> 1);
+    const bool active = ws < nwsites;
+    uint64_t base = 0;
+    if (active) {
+      uint64_t b = ws;
+#pragma unroll
+      for (int j = 0; j < 4; j++) b = ins0(b, g.hpos[j]);
+      base = (b << 5) | lane | (static_cast<uint64_t>(half) << (g.hpos[3] + 5));
+    }
+    auto vec_of = [&](int l) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < 3; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      return v;
+    };
+    float4 P[NV], L[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      if (active) {
+        const uint64_t v = vec_of(l);
+        P[l] = psi[v];
+        L[l] = lam[v];
+      } else {
+        P[l] = L[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+      }
+    }
+    if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
+#pragma unroll
+    for (int k = 0; k < NL; k++)
+      lane_ops<M, NV, C0, G0, C1, G1>(P, L, g.lbit[k], lane, g.ml[k], accf + LANE0 + M * k);
+    reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
+    reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
+    reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
+    accf[REG0 + 3 * M] += split_one<C0, G0>(P, L, mine_p, mine_l, oth_p, oth_l, half != 0,
+                                            warp >> 1, g.mh[3][0]);
+    if constexpr (M > 1)
+      accf[REG0 + 3 * M + 1] += split_one<C1, G1>(P, L, mine_p, mine_l, oth_p, oth_l,
+                                                  half != 0, warp >> 1, g.mh[3][1]);
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        const uint64_t v = vec_of(l);
+        psi[v] = P[l];
+        lam[v] = L[l];
+      }
+    }
+  }
+  double acc[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) acc[t] = accf[t];
+  finish<NOPS>(acc, NOPS, a, out);
+}
+
+// KH <= 3 register wires on one warp, optionally with wire 0 and the five
+// lane wires.
+template <int KH, bool W0, int NL, int M, int C0, int G0, int C1, int G1>
+__global__ void __launch_bounds__(kThreads, 2)
+k_adj_warp_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, UniArgs g,
+               Area a, OutSlots<M *((W0 ? 1 : 0) + NL + KH)> out) {
+  constexpr int NV = 1 << KH;
+  constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + KH);
+  constexpr int LANE0 = M * (W0 ? 1 : 0), REG0 = LANE0 + M * NL;
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
+  const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
+  float accf[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
+  for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
+    uint64_t b = ws;
+#pragma unroll
+    for (int j = 0; j < KH; j++) b = ins0(b, g.hpos[j]);
+    const uint64_t base = (b << 5) | lane;
+    float4 P[NV], L[NV];
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      P[l] = psi[v];
+      L[l] = lam[v];
+    }
+    if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
+#pragma unroll
+    for (int k = 0; k < NL; k++)
+      lane_ops<M, NV, C0, G0, C1, G1>(P, L, g.lbit[k], lane, g.ml[k], accf + LANE0 + M * k);
+    if constexpr (KH > 0) reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
+    if constexpr (KH > 1) reg_ops<M, NV, (KH > 1 ? 1 : 0), C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
+    if constexpr (KH > 2) reg_ops<M, NV, (KH > 2 ? 2 : 0), C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      uint64_t v = base;
+#pragma unroll
+      for (int j = 0; j < KH; j++)
+        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+      psi[v] = P[l];
+      lam[v] = L[l];
+    }
+  }
+  double acc[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) acc[t] = accf[t];
+  finish<NOPS>(acc, NOPS, a, out);
+}
+
+template <bool W0, int NL, int M, int C0, int G0, int C1, int G1>
+int launch_pair(float4 *psi, float4 *lam, uint64_t nw, const UniArgs &g, double *grad,
+                const uint32_t *slots, Area a, cudaStream_t s) {
+  constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + 4);
+  OutSlots<NOPS> out{};
+  out.p = grad;
+  for (int t = 0; t < NOPS; t++) out.slot[t] = slots[t];
+  unsigned grid = grid_for(nw, kThreads / 64);
+  grid = std::min<unsigned>(grid, reduce_grid());
+  const size_t smem = static_cast<size_t>(kThreads / 32) * 2 * kPairNV * 32 * sizeof(float4);
+  // The opt-in above 48 KiB is per device; set it once on each.
+  static bool opted[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (!opted[dev]) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_adj_pair_uni<W0, NL, M, C0, G0, C1, G1>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    opted[dev] = true;
+  }
+  k_adj_pair_uni<W0, NL, M, C0, G0, C1, G1><<<grid, kThreads, smem, s>>>(psi, lam, nw, g, a, out);
+  return launch_status();
+}
+
+template <int KH, bool W0, int NL, int M, int C0, int G0, int C1, int G1>
+int launch_warp(float4 *psi, float4 *lam, uint64_t nw, const UniArgs &g, double *grad,
+                const uint32_t *slots, Area a, cudaStream_t s) {
+  constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + KH);
+  OutSlots<NOPS> out{};
+  out.p = grad;
+  for (int t = 0; t < NOPS; t++) out.slot[t] = slots[t];
+  unsigned grid = grid_for(nw, kThreads / 32);
+  grid = std::min<unsigned>(grid, reduce_grid());
+  k_adj_warp_uni<KH, W0, NL, M, C0, G0, C1, G1><<<grid, kThreads, 0, s>>>(psi, lam, nw, g, a, out);
+  return launch_status();
+}
+
+// The rotation kinds a uniform tile takes: (class, generator) of RX, RY, RZ.
+constexpr int kRx = 0, kRy = 1, kRz = 2;
+int kind_of(int cls, int gen) {
+  if (cls == kMatRx && gen == 1) return kRx;
+  if (cls == kMatReal && gen == 2) return kRy;
+  if (cls == kMatDiag && gen == 3) return kRz;
+  return -1;
+}
+
+}  // namespace
+
+int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjArgs &g,
+                   const OutSlots<kMaxGen> &out, Area a, cudaStream_t s) {
+  if (kh < 1 || kh > 4 || g.nops < 1 || g.nops > 20) return 1;
+  // Wires in op order (a wire's ops are consecutive), each with its ops.
+  struct Wire {
+    int kind, arg, n;
+    int op[2];
+  };
+  Wire w[16];
+  int nwires = 0;
+  for (uint32_t o = 0; o < g.nops; o++) {
+    const int kind = g.kind[o], arg = g.arg[o];
+    if (nwires > 0 && w[nwires - 1].kind == kind && w[nwires - 1].arg == arg) {
+      Wire &c = w[nwires - 1];
+      if (c.n == 2) return 1;
+      c.op[c.n++] = static_cast<int>(o);
+      continue;
+    }
+    for (int i = 0; i < nwires; i++)
+      if (w[i].kind == kind && w[i].arg == arg) return 1;   // a wire's ops not together
+    if (nwires == 16 || kind < 0 || kind > 2) return 1;
+    w[nwires++] = {kind, arg, 1, {static_cast<int>(o), -1}};
+  }
+  const int M = w[0].n;
+  int seq[2];
+  for (int k = 0; k < M; k++) {
+    seq[k] = kind_of(g.cls[w[0].op[k]], g.gen[w[0].op[k]]);
+    if (seq[k] < 0) return 1;
+  }
+  UniArgs u{};
+  for (int j = 0; j < 4; j++) u.hpos[j] = g.hpos[j];
+  int w0 = 0, nl = 0, nh = 0;
+  uint32_t slots[20];
+  int order[16], no = 0;   // wires in kernel order: wire 0, lanes, registers by index
+  for (int i = 0; i < nwires; i++) {
+    if (w[i].n != M) return 1;
+    for (int k = 0; k < M; k++)
+      if (kind_of(g.cls[w[i].op[k]], g.gen[w[i].op[k]]) != seq[k]) return 1;
+    if (w[i].kind == 0) w0++;
+    else if (w[i].kind == 1) nl++;
+    else nh++;
+  }
+  if (w0 > 1 || nh != kh) return 1;
+  for (int i = 0; i < nwires; i++)
+    if (w[i].kind == 0) order[no++] = i;
+  for (int i = 0; i < nwires; i++)
+    if (w[i].kind == 1) order[no++] = i;
+  for (int j = 0; j < kh; j++) {
+    int found = -1;
+    for (int i = 0; i < nwires; i++)
+      if (w[i].kind == 2 && w[i].arg == j) found = i;
+    if (found < 0) return 1;
+    order[no++] = found;
+  }
+  int t = 0, li = 0;
+  for (int q = 0; q < no; q++) {
+    const Wire &c = w[order[q]];
+    for (int k = 0; k < M; k++) {
+      const int o = c.op[k];
+      slots[t++] = out.slot[g.slotidx[o]];
+      if (c.kind == 0) u.m0[k] = g.m[o];
+      else if (c.kind == 1) u.ml[li][k] = g.m[o];
+      else u.mh[c.arg][k] = g.m[o];
+    }
+    if (c.kind == 1) u.lbit[li++] = static_cast<uint32_t>(c.arg);
+  }
+  const bool wide = w0 == 1 && nl == 5, narrow = w0 == 0 && nl == 0;
+  if (!wide && !narrow) return 1;
+  double *p = out.p;
+  if (M == 1 && kh == 4) {
+    if (wide) {
+      if (seq[0] == kRx) return launch_pair<true, 5, 1, kMatRx, 1, 0, 0>(psi, lam, nw, u, p, slots, a, s);
+      if (seq[0] == kRy) return launch_pair<true, 5, 1, kMatReal, 2, 0, 0>(psi, lam, nw, u, p, slots, a, s);
+      return launch_pair<true, 5, 1, kMatDiag, 3, 0, 0>(psi, lam, nw, u, p, slots, a, s);
+    }
+    if (seq[0] == kRx) return launch_pair<false, 0, 1, kMatRx, 1, 0, 0>(psi, lam, nw, u, p, slots, a, s);
+    if (seq[0] == kRy) return launch_pair<false, 0, 1, kMatReal, 2, 0, 0>(psi, lam, nw, u, p, slots, a, s);
+    return launch_pair<false, 0, 1, kMatDiag, 3, 0, 0>(psi, lam, nw, u, p, slots, a, s);
+  }
+  if (M == 2 && kh == 4 && narrow) {
+    if (seq[0] == kRz && seq[1] == kRy)
+      return launch_pair<false, 0, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+    if (seq[0] == kRy && seq[1] == kRz)
+      return launch_pair<false, 0, 2, kMatReal, 2, kMatDiag, 3>(psi, lam, nw, u, p, slots, a, s);
+    return 1;
+  }
+  if (M == 1 && seq[0] == kRx && kh <= 3) {
+#define QMK_UNI_RX(KH)                                                                        \
+  if (kh == KH) {                                                                             \
+    if (wide) return launch_warp<KH, true, 5, 1, kMatRx, 1, 0, 0>(psi, lam, nw, u, p, slots, a, s); \
+    return launch_warp<KH, false, 0, 1, kMatRx, 1, 0, 0>(psi, lam, nw, u, p, slots, a, s);   \
+  }
+    QMK_UNI_RX(1)
+    QMK_UNI_RX(2)
+    QMK_UNI_RX(3)
+#undef QMK_UNI_RX
+  }
+  if (M == 2 && seq[0] == kRz && seq[1] == kRy && kh <= 3) {
+    if (wide && kh == 2)
+      return launch_warp<2, true, 5, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+    if (narrow && kh == 1)
+      return launch_warp<1, false, 0, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+    if (narrow && kh == 2)
+      return launch_warp<2, false, 0, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+    if (narrow && kh == 3)
+      return launch_warp<3, false, 0, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
+  }
+  return 1;
+}
+
+}  // namespace qmk_adj

@@ -41,6 +41,12 @@ __device__ __forceinline__ float overlap(int gen, float2 p0, float2 p1, float2 l
   return (l0.x * w0.y - l0.y * w0.x) + (l1.x * w1.y - l1.y * w1.x);
 }
 
+// The backward pass of a window tile whose wires all carry the same short
+// rotation sequence (k_adjoint_uniform.cu). Returns 1 with nothing launched
+// when the tile is not of that form, else 0 or a CUDA error code.
+int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArgs &g,
+                   const qmk::OutSlots<kMaxGen> &slots, qmk::Area a, cudaStream_t s);
+
 // Launch the backward pass of one window tile: kh wires >= 6 in registers
 // (four: a warp pair), ng gradient slots (0, 4, 8 or 16). Returns 0 or a CUDA
 // error code.
