@@ -487,6 +487,29 @@ def test_uniform_rotation_layers(n):
     assert np.abs(np.array(g2) - g0).max() <= 1e-5
 
 
+@pytest.mark.parametrize("n", list(range(7, 16)))
+def test_uniform_tile_shapes_every_width(n):
+    """Every width from 7 to 15 leaves a different remainder of register
+    wires for the last tile of a layer (one to four, on one warp or a warp
+    pair): an RX layer, an RY.RZ layer (RZ then RY backward) and an RZ.RY
+    layer, against the oracle's adjoint."""
+    rng = np.random.default_rng(1300 + n)
+    ang = lambda: float(rng.uniform(-3, 3))
+    entangle = [(CX, (q, q + 1), ()) for q in range(n - 1)]
+    gates = [(H, (q,), ()) for q in range(n)] + entangle
+    gates += [(RX, (q,), (ang(),)) for q in range(n)] + entangle
+    for q in range(n):
+        gates += [(RY, (q,), (ang(),)), (RZ, (q,), (ang(),))]
+    gates += entangle
+    for q in range(n):
+        gates += [(RZ, (q,), (ang(),)), (RY, (q,), (ang(),))]
+    terms = W.ring_tfim_hamiltonian(n, 0.7)
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    e1, g1 = qm.Simulator(n).energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+    assert abs(e1 - e0) <= 1e-5
+    assert np.abs(np.array(g1) - g0).max() <= 1e-5
+
+
 def test_gradient_matches_oracle_adjoint_wide():
     """All gate kinds in the backward sweep, every wire, n = 12."""
     n = 12
