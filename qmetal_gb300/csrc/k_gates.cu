@@ -178,6 +178,86 @@ k_group(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
   }
 }
 
+// Five wires >= 1 on a warp pair: a site's 32 vectors are split by the bit
+// of the fifth wire between the two warps of a pair, each thread holding 16
+// in registers (half the registers of k_group<5>, so two blocks fit per SM
+// and twice the warps hide the loads). Ops on the first four wires pair
+// registers; the fifth trades vectors through shared memory and each thread
+// updates its own half. A pair covers 32 consecutive sites (lane = site).
+constexpr int kPairVecs = 16;
+
+__device__ __forceinline__ void group_pair_sync(uint32_t p) {
+  asm volatile("bar.sync %0, 64;" ::"r"(p + 1) : "memory");
+}
+
+template <bool W0, int CLS>
+__global__ void __launch_bounds__(kThreads, 2)
+k_group5_pair(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
+  constexpr int NV = kPairVecs;
+  extern __shared__ __align__(16) float4 xg[];   // [warp][NV][32 lanes]
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t half = warp & 1, pair = warp >> 1;
+  const uint64_t s = (static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) + pair) * 32 + lane;
+  // Both warps of a pair reach the exchange barrier: the pair's 32 sites
+  // are all valid or all invalid (nsites is a multiple of 32 here).
+  const bool active = s < nsites;
+  uint64_t base = s;
+#pragma unroll
+  for (int j = 0; j < 5; j++) base = ins0(base, g.pos[j]);
+  base |= static_cast<uint64_t>(half) << g.pos[4];
+  auto vec_of = [&](int l) {
+    uint64_t v = base;
+#pragma unroll
+    for (int j = 0; j < 4; j++)
+      if ((l >> j) & 1) v |= 1ull << g.pos[j];
+    return v;
+  };
+  float4 r[NV];
+#pragma unroll
+  for (int l = 0; l < NV; l++) r[l] = active ? st[vec_of(l)] : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (W0) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      float2 x = lo2(r[l]), y = hi2(r[l]);
+      apply2c(CLS, g.m0, x, y);
+      r[l] = pack4(x, y);
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < 4; j++) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      if ((l >> j) & 1) continue;
+      const int h = l | (1 << j);
+      float2 a0 = lo2(r[l]), b0 = lo2(r[h]), a1 = hi2(r[l]), b1 = hi2(r[h]);
+      apply2c(CLS, g.m[j], a0, b0);
+      apply2c(CLS, g.m[j], a1, b1);
+      r[l] = pack4(a0, a1);
+      r[h] = pack4(b0, b1);
+    }
+  }
+  // The fifth wire: own' = s own + t other, (a, b) on its 0 side, (d, c) on
+  // its 1 side.
+  float4 *mine = xg + warp * NV * 32 + lane;
+  const float4 *other = xg + (warp ^ 1) * NV * 32 + lane;
+  if (CLS != kMatDiag) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) mine[l * 32] = r[l];
+    group_pair_sync(pair);
+  }
+  const M2 &m = g.m[4];
+  const float2 cs = half ? m.d : m.a, ct = half ? m.c : m.b;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    const float4 o = CLS != kMatDiag ? other[l * 32] : r[l];
+    r[l] = pack4(cmac2c(CLS, cs, lo2(r[l]), ct, lo2(o)), cmac2c(CLS, cs, hi2(r[l]), ct, hi2(o)));
+  }
+  if (active) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) st[vec_of(l)] = r[l];
+  }
+}
+
 struct WarpGroupArgs {
   uint32_t nlow;     // wires 1..5: lane bits
   uint32_t lbit[5];  // their vector bits (0..4)
@@ -553,6 +633,35 @@ static void launch_group(float4 *st, uint64_t nsites, const GroupArgs &g, int cl
   }
 }
 
+template <bool W0, int CLS>
+static int launch_group5_pair_cls(float4 *st, uint64_t nsites, const GroupArgs &g,
+                                  cudaStream_t s) {
+  const size_t smem = static_cast<size_t>(kThreads / 32) * kPairVecs * 32 * sizeof(float4);
+  // The opt-in above 48 KiB is per device; set it once on each.
+  static bool opted[64] = {};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (!opted[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_group5_pair<W0, CLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    opted[dev] = true;
+  }
+  k_group5_pair<W0, CLS><<<grid_for(nsites, kThreads / 2), kThreads, smem, s>>>(st, nsites, g);
+  return launch_status();
+}
+
+template <bool W0>
+static int launch_group5_pair(float4 *st, uint64_t nsites, const GroupArgs &g, int cls,
+                              cudaStream_t s) {
+  switch (cls) {
+    case kMatDiag: return launch_group5_pair_cls<W0, kMatDiag>(st, nsites, g, s);
+    case kMatRx: return launch_group5_pair_cls<W0, kMatRx>(st, nsites, g, s);
+    case kMatReal: return launch_group5_pair_cls<W0, kMatReal>(st, nsites, g, s);
+    default: return launch_group5_pair_cls<W0, kMatGeneral>(st, nsites, g, s);
+  }
+}
+
 template <int KH, bool W0>
 static void launch_group_warp(float4 *st, uint64_t nw, const WarpGroupArgs &g, int cls,
                               unsigned grid, cudaStream_t s) {
@@ -645,8 +754,15 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
     case 7: launch_group<3, true>(st, nsites, g, cls, s); break;
     case 8: launch_group<4, false>(st, nsites, g, cls, s); break;
     case 9: launch_group<4, true>(st, nsites, g, cls, s); break;
-    case 10: launch_group<5, false>(st, nsites, g, cls, s); break;
-    case 11: launch_group<5, true>(st, nsites, g, cls, s); break;
+    // Five register wires: on warp pairs once a pair's 32 sites exist.
+    case 10:
+      if (nsites >= 32) return launch_group5_pair<false>(st, nsites, g, cls, s);
+      launch_group<5, false>(st, nsites, g, cls, s);
+      break;
+    case 11:
+      if (nsites >= 32) return launch_group5_pair<true>(st, nsites, g, cls, s);
+      launch_group<5, true>(st, nsites, g, cls, s);
+      break;
     default: return -1;
   }
   return launch_status();

@@ -57,7 +57,23 @@ def _route_cases(n, rng):
         for k in range(1, min(5, n - 6) + 1):
             high = sorted(rng.choice(np.arange(6, n), size=k, replace=False).tolist())
             cases.append([0] + high)
+    # five wires >= 1 without wire 0 (on warp pairs from n = 11), including
+    # lane wires
+    if n >= 11:
+        cases.append(sorted(rng.choice(np.arange(6, n), size=5, replace=False).tolist()))
+        cases.append([1, 3] + sorted(rng.choice(np.arange(6, n), size=3, replace=False).tolist()))
     return cases
+
+
+def _structured(rng, kind):
+    """A 2x2 of one structure class: RX-like, real (RY-like), diagonal."""
+    t = rng.uniform(-3, 3)
+    c, s = np.cos(t / 2), np.sin(t / 2)
+    if kind == "rx":
+        return np.array([[c, -1j * s], [-1j * s, c]])
+    if kind == "real":
+        return np.array([[c, -s], [s, c]])
+    return np.diag([np.exp(-0.5j * t), np.exp(0.5j * t)])
 
 
 @pytest.mark.parametrize("n", [6, 7, 9, 10, 11, 14])
@@ -70,8 +86,11 @@ def test_every_route_matches_complex128(n):
     host = np.empty(2 << n, dtype=np.float32)
     host[0::2] = init.real
     host[1::2] = init.imag
-    for wires in _route_cases(n, rng):
-        mats = [_unitary(rng) for _ in wires]
+    cases = [(w, "general") for w in _route_cases(n, rng)]
+    cases += [(w, kind) for w in _route_cases(n, rng) if len(w) >= 5
+              for kind in ("rx", "real", "diag")]
+    for wires, kind in cases:
+        mats = [_unitary(rng) if kind == "general" else _structured(rng, kind) for _ in wires]
         flat = np.empty(8 * len(wires), dtype=np.float32)
         for j, m in enumerate(mats):
             flat[8 * j:8 * j + 8] = [m[0, 0].real, m[0, 0].imag, m[0, 1].real, m[0, 1].imag,
