@@ -4,9 +4,9 @@
 // TFIM circuits -- or RZ then RY, the backward order of a hardware-efficient
 // layer). With the sequence known there is no per-op dispatch, the gradient
 // partials sit in registers at fixed indices, and the compiler may interleave
-// one op's shuffles with another's arithmetic. The per-op arithmetic and the
-// op order are those of the general tiles (k_adjoint_tiles.cu), so results
-// are the same bits.
+// one op's shuffles with another's arithmetic. The per-op arithmetic is that
+// of the general tiles (k_adjoint_tiles.cu, through kadjoint_ops.cuh); the
+// pipelined warp-pair tiles run the split wire's ops first.
 #include <algorithm>
 
 #include "kadjoint_ops.cuh"
@@ -70,8 +70,29 @@ __device__ __forceinline__ float split_one(float4 (&P)[kPairNV], float4 (&L)[kPa
   return ov;
 }
 
+// 16-byte asynchronous copy global -> shared (no registers held while it
+// is in flight) and the wait for all of this thread's copies.
+__device__ __forceinline__ void cp_async16(float4 *smem_dst, const float4 *src) {
+  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() {
+  asm volatile("cp.async.wait_group 0;" ::: "memory");
+}
+
 // Four register wires on a warp pair (the fourth split across the pair),
-// optionally with wire 0 and the five lane wires.
+// optionally with wire 0 and the five lane wires. With the op list this
+// short the tile is bound by load latency; where a round has enough work to
+// hide a load behind (two ops per wire, or the ten-wire tile), each
+// thread's vectors for the next round stream into its own shared-memory
+// slots while the current round computes: a round reads its slots, runs the
+// split wire's ops first (they commute with the other wires' ops; their
+// exchanges go through the same slots), then sends out the next round's
+// copies and runs the rest. The four-op tile loads directly (measured: the
+// staging costs it more than it hides).
 template <bool W0, int NL, int M, int C0, int G0, int C1, int G1>
 __global__ void __launch_bounds__(kThreads, 2)
 k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, UniArgs g,
@@ -79,6 +100,7 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   constexpr int NV = kPairNV;
   constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + 4);
   constexpr int LANE0 = M * (W0 ? 1 : 0), REG0 = LANE0 + M * NL;
+  constexpr bool kPipe = M > 1 || W0;
   extern __shared__ __align__(16) float4 xs[];   // [warp][state][NV][32 lanes]
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t half = warp & 1;
@@ -91,34 +113,68 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   float accf[NOPS];
 #pragma unroll
   for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
-  for (uint64_t r = 0; r < rounds; r++) {
-    const uint64_t ws = r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) +
-                        (warp >> 1);
-    const bool active = ws < nwsites;
-    uint64_t base = 0;
-    if (active) {
-      uint64_t b = ws;
+  auto site = [&](uint64_t r) {
+    return r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) + (warp >> 1);
+  };
+  auto base_of = [&](uint64_t ws) {
+    uint64_t b = ws;
 #pragma unroll
-      for (int j = 0; j < 4; j++) b = ins0(b, g.hpos[j]);
-      base = (b << 5) | lane | (static_cast<uint64_t>(half) << (g.hpos[3] + 5));
+    for (int j = 0; j < 4; j++) b = ins0(b, g.hpos[j]);
+    return (b << 5) | lane | (static_cast<uint64_t>(half) << (g.hpos[3] + 5));
+  };
+  auto vec_of = [&](uint64_t base, int l) {
+    uint64_t v = base;
+#pragma unroll
+    for (int j = 0; j < 3; j++)
+      if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
+    return v;
+  };
+  auto prefetch = [&](uint64_t r) {
+    const uint64_t ws = site(r);
+    if (r < rounds && ws < nwsites) {
+      const uint64_t base = base_of(ws);
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        const uint64_t v = vec_of(base, l);
+        cp_async16(mine_p + l * 32, psi + v);
+        cp_async16(mine_l + l * 32, lam + v);
+      }
     }
-    auto vec_of = [&](int l) {
-      uint64_t v = base;
-#pragma unroll
-      for (int j = 0; j < 3; j++)
-        if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
-      return v;
-    };
+    cp_async_commit();
+  };
+  if constexpr (kPipe) prefetch(0);
+  for (uint64_t r = 0; r < rounds; r++) {
+    const uint64_t ws = site(r);
+    const bool active = ws < nwsites;
+    const uint64_t base = active ? base_of(ws) : 0;
+    if constexpr (kPipe) cp_async_wait_all();
     float4 P[NV], L[NV];
 #pragma unroll
     for (int l = 0; l < NV; l++) {
-      if (active) {
-        const uint64_t v = vec_of(l);
+      if (!active) {
+        P[l] = L[l] = make_float4(0.f, 0.f, 0.f, 0.f);
+      } else if (kPipe) {
+        P[l] = mine_p[l * 32];
+        L[l] = mine_l[l * 32];
+      } else {
+        const uint64_t v = vec_of(base, l);
         P[l] = psi[v];
         L[l] = lam[v];
-      } else {
-        P[l] = L[l] = make_float4(0.f, 0.f, 0.f, 0.f);
       }
+    }
+    auto split_ops = [&]() {
+      accf[REG0 + 3 * M] += split_one<C0, G0>(P, L, mine_p, mine_l, oth_p, oth_l, half != 0,
+                                              warp >> 1, g.mh[3][0]);
+      if constexpr (M > 1)
+        accf[REG0 + 3 * M + 1] += split_one<C1, G1>(P, L, mine_p, mine_l, oth_p, oth_l,
+                                                    half != 0, warp >> 1, g.mh[3][1]);
+    };
+    // Pipelined: the split wire's ops first. They rewrite all of P and L, so
+    // by their end this thread's slot reads are done; the partner's reads of
+    // its slots end at the barrier that closes an exchange.
+    if constexpr (kPipe) {
+      split_ops();
+      prefetch(r + 1);
     }
     if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
 #pragma unroll
@@ -127,20 +183,17 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
     reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
     reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
-    accf[REG0 + 3 * M] += split_one<C0, G0>(P, L, mine_p, mine_l, oth_p, oth_l, half != 0,
-                                            warp >> 1, g.mh[3][0]);
-    if constexpr (M > 1)
-      accf[REG0 + 3 * M + 1] += split_one<C1, G1>(P, L, mine_p, mine_l, oth_p, oth_l,
-                                                  half != 0, warp >> 1, g.mh[3][1]);
+    if constexpr (!kPipe) split_ops();
     if (active) {
 #pragma unroll
       for (int l = 0; l < NV; l++) {
-        const uint64_t v = vec_of(l);
+        const uint64_t v = vec_of(base, l);
         psi[v] = P[l];
         lam[v] = L[l];
       }
     }
   }
+  if constexpr (kPipe) cp_async_wait_all();
   double acc[NOPS];
 #pragma unroll
   for (int t = 0; t < NOPS; t++) acc[t] = accf[t];
