@@ -3,6 +3,7 @@
 // reverse with the overlap of every rotation taken first. Split from
 // k_adjoint.cu so the two compile in parallel.
 #include <algorithm>
+#include <atomic>
 
 #include "kadjoint_ops.cuh"
 
@@ -183,7 +184,7 @@ int launch_adj_pair(float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArg
   grid = std::min<unsigned>(grid, reduce_grid());
   const size_t smem = static_cast<size_t>(kThreads / 32) * 2 * kPairNV * 32 * sizeof(float4);
   // The opt-in above 48 KiB is per device; set it once on each.
-  static bool opted[64] = {};
+  static std::atomic<bool> opted[64];   // zero-initialised: false
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
   if (!opted[dev]) {

@@ -8,6 +8,7 @@
 // of the general tiles (k_adjoint_tiles.cu, through kadjoint_ops.cuh); the
 // pipelined warp-pair tiles run the split wire's ops first.
 #include <algorithm>
+#include <atomic>
 
 #include "kadjoint_ops.cuh"
 
@@ -264,7 +265,7 @@ int launch_pair(float4 *psi, float4 *lam, uint64_t nw, const UniArgs &g, double 
   grid = std::min<unsigned>(grid, reduce_grid());
   const size_t smem = static_cast<size_t>(kThreads / 32) * 2 * kPairNV * 32 * sizeof(float4);
   // The opt-in above 48 KiB is per device; set it once on each.
-  static bool opted[64] = {};
+  static std::atomic<bool> opted[64];   // zero-initialised: false
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
   if (!opted[dev]) {

@@ -8,6 +8,7 @@
 // spaced kThreads apart (loads for all U first, then math, then stores) so
 // enough bytes are in flight to cover HBM latency.
 #include <algorithm>
+#include <atomic>
 #include <cstring>
 #include <vector>
 
@@ -638,7 +639,7 @@ static int launch_group5_pair_cls(float4 *st, uint64_t nsites, const GroupArgs &
                                   cudaStream_t s) {
   const size_t smem = static_cast<size_t>(kThreads / 32) * kPairVecs * 32 * sizeof(float4);
   // The opt-in above 48 KiB is per device; set it once on each.
-  static bool opted[64] = {};
+  static std::atomic<bool> opted[64];   // zero-initialised: false
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
   if (!opted[dev]) {
