@@ -729,6 +729,21 @@ def main():
                          "norm": big.norm(), "z0": big.expectation_pauli(z_mask=1)}
                 if name == "ghz":
                     entry["z0_zlast"] = big.expectation_pauli(z_mask=1 | (1 << (ns - 1)))
+                # The merged executor: GHZ's CX chain and QFT's closing
+                # swaps become one permutation pass each (a second state
+                # buffer, taken while the device has room).
+                big.reset()
+                big.run_merged(c)
+                big.synchronize()
+                big.elapsed()
+                big.reset()
+                big.run_merged(c)
+                tm = big.elapsed()
+                entry["merged"] = {"s_per_circuit": round(tm, 4), "norm": big.norm(),
+                                   "z0": big.expectation_pauli(z_mask=1)}
+                if name == "ghz":
+                    entry["merged"]["z0_zlast"] = big.expectation_pauli(
+                        z_mask=1 | (1 << (ns - 1)))
                 scale[f"{name}_{ns}"] = entry
             big.close()
             del big
