@@ -71,8 +71,10 @@ int qmk_apply_swap(float *state, uint32_t n, uint32_t a, uint32_t b,
  * invertible). A run of CX / SWAP / X gates is such a map, so the run costs
  * one pass instead of one per gate; it replaces consecutive
  * apply_controlled_1q / apply_swap dispatches (simulator.mm:526-547) and has
- * no single counterpart there. dst and src must not overlap. Returns -1 for
- * a singular map or bad arguments, without launching. */
+ * no single counterpart there. The pass runs as that gather or as the
+ * equivalent scatter through G^-1, whichever map spreads a warp's accesses
+ * further. dst and src must not overlap. Returns -1 for a singular map or
+ * bad arguments, without launching. */
 int qmk_apply_permutation(float *dst, const float *src, uint32_t n,
                           const uint64_t *cols, uint64_t offset, void *stream);
 
