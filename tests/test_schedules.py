@@ -323,7 +323,7 @@ def random_terms(n, count, seed):
     out = []
     for _ in range(count):
         x = y = z = 0
-        for q in rng.choice(n, int(rng.integers(1, 4)), replace=False):
+        for q in rng.choice(n, int(rng.integers(1, min(4, n + 1))), replace=False):
             k = int(rng.integers(3))
             x |= (k == 0) << int(q)
             y |= (k == 1) << int(q)
@@ -442,3 +442,51 @@ def test_schedule_export_errors():
         c.schedule_export("costate")
     with pytest.raises(KeyError):
         c.schedule_export("sideways")
+
+
+# --- property tests (hypothesis; skipped where it is not installed) -----------
+
+def _gate_strategy(st, n):
+    one = st.tuples(st.sampled_from([X, Y, Z, H, S, SDG, T, TDG]), st.integers(0, n - 1)).map(
+        lambda t: (t[0], (t[1],), ()))
+    rot = st.tuples(st.sampled_from([RX, RY, RZ]), st.integers(0, n - 1),
+                    st.floats(-3.0, 3.0, allow_nan=False)).map(lambda t: (t[0], (t[1],), (t[2],)))
+    pair = st.tuples(st.sampled_from([CX, CY, CZ, SWAP]), st.integers(0, n - 1),
+                     st.integers(1, n - 1)).map(lambda t: (t[0], (t[1], (t[1] + t[2]) % n), ()))
+    zz = st.tuples(st.integers(0, n - 1), st.integers(1, n - 1),
+                   st.floats(-2.0, 2.0, allow_nan=False)).map(
+        lambda t: [(CX, (t[0], (t[0] + t[1]) % n), ()), (RZ, ((t[0] + t[1]) % n,), (t[2],)),
+                   (CX, (t[0], (t[0] + t[1]) % n), ())])
+    ladder = st.integers(2, n).map(lambda k: [(CX, (i, i + 1), ()) for i in range(k - 1)])
+    return st.lists(st.one_of(one.map(lambda g: [g]), rot.map(lambda g: [g]),
+                              pair.map(lambda g: [g]), zz, ladder), min_size=4, max_size=30
+                    ).map(lambda chunks: [g for c in chunks for g in c])
+
+
+def test_random_circuits_replay_property():
+    """Random circuits of every gate kind (rotations, fixed one-qubit gates,
+    couplings, CX ladders, swaps) and random Hamiltonians: the forward
+    schedule reproduces the gate-by-gate state and the backward schedule the
+    adjoint gradient, for every tile shape."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=80, deadline=None, derandomize=True)
+    @hyp.given(st.data())
+    def check(data):
+        n = data.draw(st.integers(2, 9))
+        gates = data.draw(_gate_strategy(st, n))
+        seed = data.draw(st.integers(0, 2**31 - 1))
+        terms = random_terms(n, 5, seed) + one_flip_terms(n, seed)[:4]
+        state, _ = replay_forward(n, gates)
+        assert np.abs(state - oracle.run(n, gates)).max() < 1e-12
+        tile_high = data.draw(st.integers(1, 4))
+        grad, touched, _ = replay_backward(n, gates, terms, tile_high)
+        _, want = oracle.energy_and_gradient(n, gates, terms)
+        assert np.abs(grad - want).max() < 1e-10
+        params = np.array([len(g[2]) > 0 for g in gates])
+        assert (touched == params).all()
+        lam, covered = replay_costate(n, oracle.run(n, gates), terms)
+        assert np.abs(lam - h_apply(oracle.run(n, gates), n, terms)).max() < 1e-12
+
+    check()
