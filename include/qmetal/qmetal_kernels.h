@@ -194,6 +194,12 @@ int qmk_adjoint_group(float *psi, float *lambda, uint32_t n, uint32_t num_ops,
                       const uint32_t *slots, double *d_grad, void *workspace,
                       size_t workspace_bytes, void *stream);
 
+/* How many bounded waits of the window-tile kernels gave up since the last
+ * call (each wait is on a bulk copy into shared memory; one that gives up
+ * leaves that pass's results invalid), and reset the count. Read it after
+ * synchronising the streams that ran the passes. 0 or a CUDA error code. */
+int qmk_take_wait_timeouts(unsigned int *out);
+
 /* Sampling workspace bytes for n qubits (block CDF in FP64). */
 size_t qmk_sample_workspace_bytes(uint32_t n);
 

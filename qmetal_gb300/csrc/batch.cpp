@@ -14,6 +14,8 @@
 // tile shape of the backward window passes per width and the lane count.
 #include "batch.hpp"
 
+#include "../../include/qmetal/qmetal_kernels.h"
+
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -221,6 +223,9 @@ void serve_graph(const std::vector<BatchItem> &items, const std::vector<size_t> 
     const cudaError_t e = cudaStreamSynchronize(origin);
     if (e != cudaSuccess) throw std::runtime_error(std::string("batch: ") + cudaGetErrorString(e));
     timing.execute_s = seconds_since(t_exec);
+    unsigned int gave_up = 0;
+    if (qmk_take_wait_timeouts(&gave_up) != 0 || gave_up)
+      throw std::runtime_error("batch: an adjoint window pass gave up a bulk-copy wait");
     for (const BatchItem &it : items) {
       const uint64_t *slot = pinned + offset[&it - items.data()];
       if (it.energy) std::memcpy(it.energy, slot, sizeof(double));

@@ -11,6 +11,7 @@
 #include <atomic>
 
 #include "kadjoint_ops.cuh"
+#include "../../include/qmetal/qmetal_kernels.h"
 
 using namespace qmk;
 using qmk_host::grid_for;
@@ -71,29 +72,69 @@ __device__ __forceinline__ float split_one(float4 (&P)[kPairNV], float4 (&L)[kPa
   return ov;
 }
 
-// 16-byte asynchronous copy global -> shared (no registers held while it
-// is in flight) and the wait for all of this thread's copies.
-__device__ __forceinline__ void cp_async16(float4 *smem_dst, const float4 *src) {
-  const uint32_t d = static_cast<uint32_t>(__cvta_generic_to_shared(smem_dst));
-  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+// Bulk copies through the TMA engine: one 512-byte row per instruction,
+// completion counted in bytes on a shared-memory mbarrier. Every wait is
+// bounded: a wait that gives up is counted in g_bulk_wait_timeouts (read by
+// the host after the pass) and the kernel goes on, so it cannot hang.
+__device__ unsigned int g_bulk_wait_timeouts;
+constexpr uint32_t kMaxWaitPolls = 1u << 22;
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
 }
-__device__ __forceinline__ void cp_async_commit() {
-  asm volatile("cp.async.commit_group;" ::: "memory");
+__device__ __forceinline__ void mbar_init(uint64_t *mb, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(mb)), "r"(count)
+               : "memory");
 }
-__device__ __forceinline__ void cp_async_wait_all() {
-  asm volatile("cp.async.wait_group 0;" ::: "memory");
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *mb, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mb)),
+               "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *mb, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(mb)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+__device__ __forceinline__ void bulk_row(void *dst, const void *src, uint32_t bytes, uint64_t *mb) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mb))
+      : "memory");
+}
+// Order this thread's earlier shared-memory accesses (and, after a barrier,
+// its partners') before the async proxy's next writes to the same bytes.
+__device__ __forceinline__ void fence_proxy_async() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_wait(uint64_t *mb, uint32_t parity) {
+  uint32_t polls = 0;
+  while (!mbar_try_wait(mb, parity)) {
+    if (++polls == kMaxWaitPolls) {
+      if ((threadIdx.x & 31) == 0) atomicAdd(&g_bulk_wait_timeouts, 1u);
+      break;
+    }
+  }
 }
 
 // Four register wires on a warp pair (the fourth split across the pair),
 // optionally with wire 0 and the five lane wires. With the op list this
 // short the tile is bound by load latency; where a round has enough work to
-// hide a load behind (two ops per wire, or the ten-wire tile), each
-// thread's vectors for the next round stream into its own shared-memory
-// slots while the current round computes: a round reads its slots, runs the
-// split wire's ops first (they commute with the other wires' ops; their
-// exchanges go through the same slots), then sends out the next round's
-// copies and runs the rest. The four-op tile loads directly (measured: the
-// staging costs it more than it hides).
+// hide a load behind (two ops per wire, or the ten-wire tile), the warp's
+// vectors for the next round stream into its shared-memory slots while the
+// current round computes, as 16 bulk copies of one 512-byte row each issued
+// by one lane: a round reads its slots, runs the split wire's ops first
+// (they commute with the other wires' ops; their exchanges go through the
+// same slots), then sends out the next round's copies and runs the rest.
+// The four-op tile loads directly (measured: the staging costs it more
+// than it hides).
 template <bool W0, int NL, int M, int C0, int G0, int C1, int G1>
 __global__ void __launch_bounds__(kThreads, 2)
 k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsites, UniArgs g,
@@ -130,25 +171,42 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
       if ((l >> j) & 1) v |= 1ull << (g.hpos[j] + 5);
     return v;
   };
+  __shared__ uint64_t mbar[kThreads / 32];   // one per warp: its next round's rows
+  uint32_t parity = 0;
+  if constexpr (kPipe) {
+    if (lane == 0) mbar_init(&mbar[warp], 1);
+    fence_proxy_async();
+    __syncwarp();
+  }
+  // The next round's rows of this warp (8 of each state), if it has one.
   auto prefetch = [&](uint64_t r) {
     const uint64_t ws = site(r);
     if (r < rounds && ws < nwsites) {
-      const uint64_t base = base_of(ws);
+      const uint64_t row0 = base_of(ws) & ~31ull;
+      __syncwarp();
+      if (lane == 0) {
+        fence_proxy_async();
+        mbar_expect_tx(&mbar[warp], 2 * NV * 32 * sizeof(float4));
 #pragma unroll
-      for (int l = 0; l < NV; l++) {
-        const uint64_t v = vec_of(base, l);
-        cp_async16(mine_p + l * 32, psi + v);
-        cp_async16(mine_l + l * 32, lam + v);
+        for (int l = 0; l < NV; l++) {
+          const uint64_t v = vec_of(row0, l);
+          bulk_row(mine_p - lane + l * 32, psi + v, 32 * sizeof(float4), &mbar[warp]);
+          bulk_row(mine_l - lane + l * 32, lam + v, 32 * sizeof(float4), &mbar[warp]);
+        }
       }
     }
-    cp_async_commit();
   };
   if constexpr (kPipe) prefetch(0);
   for (uint64_t r = 0; r < rounds; r++) {
     const uint64_t ws = site(r);
     const bool active = ws < nwsites;
     const uint64_t base = active ? base_of(ws) : 0;
-    if constexpr (kPipe) cp_async_wait_all();
+    if constexpr (kPipe) {
+      if (active) {
+        mbar_wait(&mbar[warp], parity);
+        parity ^= 1u;
+      }
+    }
     float4 P[NV], L[NV];
 #pragma unroll
     for (int l = 0; l < NV; l++) {
@@ -194,7 +252,6 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
       }
     }
   }
-  if constexpr (kPipe) cp_async_wait_all();
   double acc[NOPS];
 #pragma unroll
   for (int t = 0; t < NOPS; t++) acc[t] = accf[t];
@@ -302,6 +359,19 @@ int kind_of(int cls, int gen) {
 }
 
 }  // namespace
+
+int take_wait_timeouts_impl(unsigned int *out) {
+  unsigned int v = 0;
+  cudaError_t e = cudaMemcpyFromSymbol(&v, g_bulk_wait_timeouts, sizeof(v));
+  if (e != cudaSuccess) return static_cast<int>(e);
+  if (v) {
+    const unsigned int zero = 0;
+    e = cudaMemcpyToSymbol(g_bulk_wait_timeouts, &zero, sizeof(zero));
+    if (e != cudaSuccess) return static_cast<int>(e);
+  }
+  *out = v;
+  return 0;
+}
 
 int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjArgs &g,
                    const OutSlots<kMaxGen> &out, Area a, cudaStream_t s) {
@@ -414,3 +484,8 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
 }
 
 }  // namespace qmk_adj
+
+extern "C" int qmk_take_wait_timeouts(unsigned int *out) {
+  if (!out) return -1;
+  return qmk_adj::take_wait_timeouts_impl(out);
+}

@@ -595,6 +595,14 @@ void Simulator::fetch(size_t count) {
   synchronize();
 }
 
+// Fail closed if a window-tile pass gave up a bounded wait (its results are
+// not valid); call after the passes' stream is synchronised.
+void Simulator::check_waits() {
+  unsigned int n = 0;
+  check(qmk_take_wait_timeouts(&n), "wait check");
+  if (n) throw std::runtime_error("adjoint window pass: a bulk-copy wait timed out");
+}
+
 // ---------------------------------------------------------------------------
 // Reductions
 
@@ -920,6 +928,7 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
                                  S(stream_)),
                  "gradient copy");
     fetch(1);
+    check_waits();
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
     throw;
@@ -947,6 +956,7 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
                                  cudaMemcpyDeviceToHost, S(stream_)),
                  "sample copy");
     fetch(1);
+    check_waits();
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
     throw;

@@ -110,6 +110,7 @@ class Simulator {
   void sweep_gate_by_gate(const Circuit &c);
   void sweep_fused(const Circuit &c);
   void fetch(size_t count);             // d_results_ -> h_results_, sync
+  void check_waits();                   // throws if a window pass gave up a wait
   void launch_sample(size_t shots, uint64_t seed);
   // Out-of-place permutation passes need a second state-sized buffer; it is
   // allocated on first use, and only while the device has room for it.
