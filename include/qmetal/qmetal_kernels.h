@@ -194,11 +194,20 @@ int qmk_adjoint_group(float *psi, float *lambda, uint32_t n, uint32_t num_ops,
                       const uint32_t *slots, double *d_grad, void *workspace,
                       size_t workspace_bytes, void *stream);
 
-/* How many bounded waits of the window-tile kernels gave up since the last
- * call (each wait is on a bulk copy into shared memory; one that gives up
- * leaves that pass's results invalid), and reset the count. Read it after
- * synchronising the streams that ran the passes. 0 or a CUDA error code. */
-int qmk_take_wait_timeouts(unsigned int *out);
+/* How many bounded waits of the window-tile kernels that ran on `workspace`
+ * gave up since the last call (each wait is on a bulk copy into shared
+ * memory; one that gives up leaves that pass's results invalid), and reset
+ * the count: a copy on `stream` and a synchronisation of it, so call it with
+ * the stream that ran the passes. The count is the workspace's own, so
+ * callers on separate workspaces never see each other's. 0, -1 (bad
+ * arguments) or a CUDA error code. */
+int qmk_take_wait_timeouts(void *workspace, size_t workspace_bytes, unsigned int *out,
+                           void *stream);
+
+/* Device address of that count inside `workspace` (a uint32 that
+ * qmk_workspace_init zeroes and the passes only increase), for a caller that
+ * reads it with its own asynchronous copy. */
+unsigned int *qmk_wait_counter(void *workspace);
 
 /* Sampling workspace bytes for n qubits (block CDF in FP64). */
 size_t qmk_sample_workspace_bytes(uint32_t n);

@@ -223,9 +223,7 @@ void serve_graph(const std::vector<BatchItem> &items, const std::vector<size_t> 
     const cudaError_t e = cudaStreamSynchronize(origin);
     if (e != cudaSuccess) throw std::runtime_error(std::string("batch: ") + cudaGetErrorString(e));
     timing.execute_s = seconds_since(t_exec);
-    unsigned int gave_up = 0;
-    if (qmk_take_wait_timeouts(&gave_up) != 0 || gave_up)
-      throw std::runtime_error("batch: an adjoint window pass gave up a bulk-copy wait");
+    for (auto &sim : sims) sim->check_waits();
     for (const BatchItem &it : items) {
       const uint64_t *slot = pinned + offset[&it - items.data()];
       if (it.energy) std::memcpy(it.energy, slot, sizeof(double));

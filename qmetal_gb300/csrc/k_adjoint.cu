@@ -555,3 +555,20 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
 #undef QMK_ADJ_GROUP_CASE
   return launch_status();
 }
+
+extern "C" unsigned int *qmk_wait_counter(void *ws) {
+  return ws ? area_of(ws).waits : nullptr;
+}
+
+extern "C" int qmk_take_wait_timeouts(void *ws, size_t bytes, unsigned int *out, void *stream) {
+  if (!out || !ok_ws(ws, bytes, 0)) return -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  unsigned int *counter = area_of(ws).waits;
+  cudaError_t e = cudaMemcpyAsync(out, counter, sizeof(unsigned int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && *out) {
+    e = cudaMemsetAsync(counter, 0, sizeof(unsigned int), s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  }
+  return e == cudaSuccess ? 0 : static_cast<int>(e);
+}

@@ -74,9 +74,9 @@ __device__ __forceinline__ float split_one(float4 (&P)[kPairNV], float4 (&L)[kPa
 
 // Bulk copies through the TMA engine: one 512-byte row per instruction,
 // completion counted in bytes on a shared-memory mbarrier. Every wait is
-// bounded: a wait that gives up is counted in g_bulk_wait_timeouts (read by
-// the host after the pass) and the kernel goes on, so it cannot hang.
-__device__ unsigned int g_bulk_wait_timeouts;
+// bounded: a wait that gives up is counted in the workspace's wait counter
+// (Area::waits, read by the host after the pass) and the kernel goes on, so
+// it cannot hang.
 constexpr uint32_t kMaxWaitPolls = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -114,11 +114,11 @@ __device__ __forceinline__ void bulk_row(void *dst, const void *src, uint32_t by
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
-__device__ __forceinline__ void mbar_wait(uint64_t *mb, uint32_t parity) {
+__device__ __forceinline__ void mbar_wait(uint64_t *mb, uint32_t parity, unsigned *gave_up) {
   uint32_t polls = 0;
   while (!mbar_try_wait(mb, parity)) {
     if (++polls == kMaxWaitPolls) {
-      if ((threadIdx.x & 31) == 0) atomicAdd(&g_bulk_wait_timeouts, 1u);
+      if ((threadIdx.x & 31) == 0) atomicAdd(gave_up, 1u);
       break;
     }
   }
@@ -203,7 +203,7 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     const uint64_t base = active ? base_of(ws) : 0;
     if constexpr (kPipe) {
       if (active) {
-        mbar_wait(&mbar[warp], parity);
+        mbar_wait(&mbar[warp], parity, a.waits);
         parity ^= 1u;
       }
     }
@@ -360,19 +360,6 @@ int kind_of(int cls, int gen) {
 
 }  // namespace
 
-int take_wait_timeouts_impl(unsigned int *out) {
-  unsigned int v = 0;
-  cudaError_t e = cudaMemcpyFromSymbol(&v, g_bulk_wait_timeouts, sizeof(v));
-  if (e != cudaSuccess) return static_cast<int>(e);
-  if (v) {
-    const unsigned int zero = 0;
-    e = cudaMemcpyToSymbol(g_bulk_wait_timeouts, &zero, sizeof(zero));
-    if (e != cudaSuccess) return static_cast<int>(e);
-  }
-  *out = v;
-  return 0;
-}
-
 int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjArgs &g,
                    const OutSlots<kMaxGen> &out, Area a, cudaStream_t s) {
   if (kh < 1 || kh > 4 || g.nops < 1 || g.nops > 20) return 1;
@@ -484,8 +471,3 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
 }
 
 }  // namespace qmk_adj
-
-extern "C" int qmk_take_wait_timeouts(unsigned int *out) {
-  if (!out) return -1;
-  return qmk_adj::take_wait_timeouts_impl(out);
-}

@@ -19,7 +19,8 @@ constexpr uint32_t kMaxBlocks = 1024;
 
 struct Area {
   double *partials;   // kMaxBlocks x 32
-  unsigned *counter;
+  unsigned *counter;  // last-block ticket, back to 0 after each reduction
+  unsigned *waits;    // bounded waits that gave up in passes on this workspace
 };
 
 inline Area area_of(void *ws) {
@@ -27,6 +28,7 @@ inline Area area_of(void *ws) {
   Area a;
   a.partials = reinterpret_cast<double *>(b);
   a.counter = reinterpret_cast<unsigned *>(b + kMaxBlocks * 32 * sizeof(double));
+  a.waits = a.counter + 16;  // 64 bytes into the 256-byte tail, its own line
   return a;
 }
 

@@ -128,7 +128,8 @@ Simulator::Simulator(uint32_t n) : n_(n) {
     cuda_check(cudaMalloc(&state_, bytes), "Simulator: state allocation failed");
     cuda_check(cudaMalloc(&ws_, ws_bytes_), "Simulator: workspace allocation failed");
     cuda_check(cudaMalloc(&d_results_, kResultSlots * sizeof(double)), "cudaMalloc results");
-    cuda_check(cudaMallocHost(&h_results_, kResultSlots * sizeof(double)), "cudaMallocHost");
+    cuda_check(cudaMallocHost(&h_results_, (kResultSlots + 1) * sizeof(double)), "cudaMallocHost");
+    h_waits_ = reinterpret_cast<unsigned *>(h_results_ + kResultSlots);
     cudaEvent_t a, b;
     cuda_check(cudaEventCreate(&a), "cudaEventCreate");
     ev_start_ = a;
@@ -172,6 +173,7 @@ void Simulator::release() {
   ws_ = sample_ws_ = nullptr;
   d_shots_ = nullptr;
   d_results_ = h_results_ = d_grad_ = nullptr;
+  h_waits_ = nullptr;
   d_grad_cap_ = 0;
   mirror_ = nullptr;
   ev_start_ = ev_stop_ = stream_ = nullptr;
@@ -588,18 +590,28 @@ void Simulator::set_state(const float *in) {
   synchronize();
 }
 
-void Simulator::fetch(size_t count) {
+void Simulator::fetch(size_t count, bool waits) {
   cuda_check(cudaMemcpyAsync(h_results_, d_results_, count * sizeof(double),
                              cudaMemcpyDeviceToHost, S(stream_)),
              "result copy");
+  if (waits)
+    cuda_check(cudaMemcpyAsync(h_waits_, qmk_wait_counter(ws_), sizeof(unsigned),
+                               cudaMemcpyDeviceToHost, S(stream_)),
+               "wait count copy");
   synchronize();
+  // Fail closed if a window-tile pass gave up a bounded wait (its results
+  // are not valid). The counter only grows; compare with the last look.
+  if (waits && *h_waits_ != waits_seen_) {
+    waits_seen_ = *h_waits_;
+    throw std::runtime_error("adjoint window pass: a bulk-copy wait timed out");
+  }
 }
 
-// Fail closed if a window-tile pass gave up a bounded wait (its results are
-// not valid); call after the passes' stream is synchronised.
 void Simulator::check_waits() {
+  activate();
   unsigned int n = 0;
-  check(qmk_take_wait_timeouts(&n), "wait check");
+  check(qmk_take_wait_timeouts(ws_, ws_bytes_, &n, stream_), "wait check");
+  waits_seen_ = 0;  // the take reset the counter
   if (n) throw std::runtime_error("adjoint window pass: a bulk-copy wait timed out");
 }
 
@@ -927,8 +939,7 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
       cuda_check(cudaMemcpyAsync(grad.data(), d_grad_, G * sizeof(double), cudaMemcpyDeviceToHost,
                                  S(stream_)),
                  "gradient copy");
-    fetch(1);
-    check_waits();
+    fetch(1, true);
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
     throw;
@@ -955,8 +966,7 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
       cuda_check(cudaMemcpyAsync(samples, d_shots_, shots * sizeof(uint64_t),
                                  cudaMemcpyDeviceToHost, S(stream_)),
                  "sample copy");
-    fetch(1);
-    check_waits();
+    fetch(1, true);
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
     throw;

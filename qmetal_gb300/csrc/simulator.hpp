@@ -92,6 +92,10 @@ class Simulator {
   uint64_t dispatch_count() const { return dispatches_; }
   double elapsed();
 
+  // Throws if a window pass on this simulator gave up a bounded wait since
+  // the last check (a copy and a synchronisation on its stream).
+  void check_waits();
+
   static bool available();
   static std::string device_name();
   static uint64_t max_buffer_length();
@@ -109,8 +113,10 @@ class Simulator {
   double energy_and_costate(const Hamiltonian &h);
   void sweep_gate_by_gate(const Circuit &c);
   void sweep_fused(const Circuit &c);
-  void fetch(size_t count);             // d_results_ -> h_results_, sync
-  void check_waits();                   // throws if a window pass gave up a wait
+  // d_results_ -> h_results_, sync; with `waits`, also read the workspace's
+  // wait counter in the same copy batch and throw if a window pass gave up a
+  // bounded wait since the last look.
+  void fetch(size_t count, bool waits = false);
   void launch_sample(size_t shots, uint64_t seed);
   // Out-of-place permutation passes need a second state-sized buffer; it is
   // allocated on first use, and only while the device has room for it.
@@ -134,7 +140,9 @@ class Simulator {
   uint64_t *d_shots_ = nullptr;
   size_t d_shots_cap_ = 0;
   double *d_results_ = nullptr;         // kResultSlots doubles
-  double *h_results_ = nullptr;         // pinned mirror
+  double *h_results_ = nullptr;         // pinned mirror, then one wait-count slot
+  unsigned *h_waits_ = nullptr;         // inside h_results_'s last slot
+  unsigned waits_seen_ = 0;             // wait count at the last look
   double *d_grad_ = nullptr;            // adjoint gradient slots
   size_t d_grad_cap_ = 0;
   float *mirror_ = nullptr;

@@ -96,3 +96,26 @@ def test_kernel_layer_rejects_bad_arguments_without_launching():
     assert f(None, 4, 0, m, None) == -1                      # null state
     assert f(ctypes.c_void_p(16), 4, 9, m, None) == -1       # wire out of range
     assert f(ctypes.c_void_p(18), 4, 0, m, None) == -1       # misaligned
+
+
+def test_wait_counter_sits_in_the_workspace_tail():
+    """The bounded-wait count of the window tiles is per workspace: an aligned
+    uint32 inside the workspace's bytes, clear of the reduction area."""
+    lib = ctypes.CDLL(qm.library_path())
+    lib.qmk_wait_counter.restype = ctypes.c_void_p
+    lib.qmk_wait_counter.argtypes = [ctypes.c_void_p]
+    lib.qmk_workspace_bytes.restype = ctypes.c_size_t
+    lib.qmk_workspace_bytes.argtypes = [ctypes.c_uint32]
+    base = 1 << 20                     # pointer arithmetic only: nothing is dereferenced
+    ws_bytes = lib.qmk_workspace_bytes(20)
+    at = lib.qmk_wait_counter(ctypes.c_void_p(base)) - base
+    assert at % 16 == 0 and 0 < at and at + 4 <= ws_bytes
+    assert ws_bytes - at <= 256 - 64   # the tail after the 1024 x 32 FP64 partials
+    assert lib.qmk_wait_counter(None) is None
+    take = lib.qmk_take_wait_timeouts
+    take.argtypes = [ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p]
+    out = ctypes.c_uint32(7)
+    assert take(None, ws_bytes, ctypes.byref(out), None) == -1
+    assert take(ctypes.c_void_p(base), 16, ctypes.byref(out), None) == -1
+    assert take(ctypes.c_void_p(base), ws_bytes, None, None) == -1
+    assert out.value == 7
