@@ -122,7 +122,7 @@ void serve_graph(const std::vector<BatchItem> &items, const std::vector<size_t> 
                  const BatchTuning *tuning) {
   GraphTiming timing;
   const auto t_record = std::chrono::steady_clock::now();
-  // Branches: per width, split in two when it carries > 1/4 of the traffic.
+  // Branches: per width, weighted by its state traffic (2^n x ops).
   std::map<uint32_t, std::vector<size_t>> by_width;
   double total = 0.0;
   std::map<uint32_t, double> weight;

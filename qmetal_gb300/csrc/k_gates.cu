@@ -511,15 +511,18 @@ bool valid_state(const float *p, uint32_t n) {
 
 namespace qmk_host {
 int num_sms() {
-  static int cache[64] = {0};
+  // Read by every launcher, from as many host threads as there are batch
+  // lanes; a race to fill an entry only stores the same count twice.
+  static std::atomic<int> cache[64];   // zero-initialised: not yet read
   int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 148;
-  if (!cache[dev]) {
-    int v = 0;
-    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
-    cache[dev] = v > 0 ? v : 148;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 152;
+  int v = cache[dev].load(std::memory_order_relaxed);
+  if (!v) {
+    if (cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || v <= 0)
+      return 152;   // not cached: the next call asks again
+    cache[dev].store(v, std::memory_order_relaxed);
   }
-  return cache[dev];
+  return v;
 }
 }  // namespace qmk_host
 
