@@ -18,6 +18,7 @@
 // registers. Gradients land straight in the gate-indexed gradient array.
 #include <algorithm>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "kquad.cuh"
@@ -28,6 +29,7 @@
 using namespace qmk;
 using qmk_host::grid_for;
 using qmk_host::launch_status;
+using qmk_adj::kMaxDiagGen;
 using qmk_adj::kMaxGen;
 using qmk_adj::kMaxWarpOps;
 using qmk_adj::overlap;
@@ -104,10 +106,11 @@ struct DiagAdjArgs {
 };
 
 template <int T>
-__global__ void __launch_bounds__(kThreads)
-k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *__restrict__ d,
-           const float4 *__restrict__ table4, uint64_t ntiles, DiagAdjArgs<T> g, Area a,
-           OutSlots<(T > 0 ? T : 1)> out) {
+__device__ __forceinline__ void adj_diag_body(float4 *__restrict__ psi, float4 *__restrict__ lam,
+                                              const DiagDesc *__restrict__ d,
+                                              const float4 *__restrict__ table4, uint64_t ntiles,
+                                              const DiagAdjArgs<T> &g, Area a,
+                                              const OutSlots<(T > 0 ? T : 1)> &out) {
   __shared__ float2 f[kWMax];
   __shared__ float2 eH;
   __shared__ __align__(16) float2 Y1[64];
@@ -122,12 +125,14 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
   // parity of (fixed bits & fixmask[t]); the thread's own bits give a mask
   // that holds for every tile, the tile's bits one that every thread shares
   // (lane t computes bit t, a ballot hands the word to the warp).
+  // (More than 32 generators: a 64-bit sign word and a second ballot.)
+  using Sign = std::conditional_t<(T > 32), uint64_t, uint32_t>;
   __shared__ uint64_t fm[T > 0 ? T : 1];
-  uint32_t own_sign = 0;
+  Sign own_sign = 0;
   if constexpr (T > 0) {
     const uint64_t mine = static_cast<uint64_t>(tid) << 1;
     for (int t = 0; t < T && t < static_cast<int>(g.ngen); t++)
-      own_sign |= static_cast<uint32_t>(parity64(mine & g.fixmask[t])) << t;
+      own_sign |= static_cast<Sign>(parity64(mine & g.fixmask[t])) << t;
     if (tid < static_cast<uint32_t>(T)) fm[tid] = g.fixmask[tid];
   }
   __syncthreads();
@@ -205,9 +210,15 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
       const int ng = static_cast<int>(g.ngen);
       const uint64_t tbits = tile << W;
       const bool mine = static_cast<int>(lane) < ng && static_cast<int>(lane) < T;
-      const uint32_t tile_sign =
+      Sign tile_sign =
           __ballot_sync(0xffffffffu, mine && parity64(tbits & fm[lane < T ? lane : 0]));
-      const uint32_t sign = own_sign ^ tile_sign;
+      if constexpr (T > 32) {
+        const int t2 = 32 + static_cast<int>(lane);
+        const bool mine2 = t2 < ng && t2 < T;
+        const uint32_t hi = __ballot_sync(0xffffffffu, mine2 && parity64(tbits & fm[mine2 ? t2 : 0]));
+        tile_sign |= static_cast<Sign>(hi) << 32;
+      }
+      const Sign sign = own_sign ^ tile_sign;
 #pragma unroll
       for (int t = 0; t < T; t++) {
         const float v = t < ng ? row[g.vm[t]] : 0.0f;
@@ -220,6 +231,24 @@ k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *_
 #pragma unroll
   for (int t = 0; t < (T > 0 ? T : 1); t++) acc[t] = accf[t];
   if constexpr (T > 0) finish<T>(acc, g.ngen, a, out);
+}
+
+template <int T>
+__global__ void __launch_bounds__(kThreads)
+k_adj_diag(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *__restrict__ d,
+           const float4 *__restrict__ table4, uint64_t ntiles, DiagAdjArgs<T> g, Area a,
+           OutSlots<(T > 0 ? T : 1)> out) {
+  adj_diag_body<T>(psi, lam, d, table4, ntiles, g, a, out);
+}
+
+// More than 32 generators: left unbounded the kernel takes 172 registers (one
+// block a multiprocessor); held to two blocks it spills a few words.
+template <int T>
+__global__ void __launch_bounds__(kThreads, 2)
+k_adj_diag_wide(float4 *__restrict__ psi, float4 *__restrict__ lam, const DiagDesc *__restrict__ d,
+                const float4 *__restrict__ table4, uint64_t ntiles, DiagAdjArgs<T> g, Area a,
+                OutSlots<(T > 0 ? T : 1)> out) {
+  adj_diag_body<T>(psi, lam, d, table4, ntiles, g, a, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -347,11 +376,18 @@ int launch_adj_diag(float *psi, float *lam, uint32_t n, const DiagDesc *dd, cons
   }
   const uint32_t W = std::min<uint32_t>(n, kWMax);
   const uint64_t ntiles = 1ull << (n - W);
-  const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(ntiles, reduce_grid()));
-  k_adj_diag<T><<<grid, kThreads, 0, s>>>(reinterpret_cast<float4 *>(psi),
-                                           reinterpret_cast<float4 *>(lam), dd,
-                                           reinterpret_cast<const float4 *>(table), ntiles, g,
-                                           area_of(ws), out);
+  float4 *p4 = reinterpret_cast<float4 *>(psi), *l4 = reinterpret_cast<float4 *>(lam);
+  const float4 *t4 = reinterpret_cast<const float4 *>(table);
+  if constexpr (T > 32) {
+    // 64 partials a block: at most kMaxBlocks / 2 blocks; one wave of two
+    // blocks a multiprocessor.
+    const unsigned cap = std::min<unsigned>(kMaxBlocks / 2, 2u * qmk_host::num_sms());
+    const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(ntiles, cap));
+    k_adj_diag_wide<T><<<grid, kThreads, 0, s>>>(p4, l4, dd, t4, ntiles, g, area_of(ws), out);
+  } else {
+    const unsigned grid = static_cast<unsigned>(std::min<uint64_t>(ntiles, reduce_grid()));
+    k_adj_diag<T><<<grid, kThreads, 0, s>>>(p4, l4, dd, t4, ntiles, g, area_of(ws), out);
+  }
   return launch_status();
 }
 
@@ -422,7 +458,7 @@ extern "C" int qmk_adjoint_diagonal(float *psi, float *lam, uint32_t n, uint32_t
                                     size_t ws_bytes, void *stream) {
   if (!psi || !lam || n < 1 || n > 40 || (nt && (!masks || !angles)) || !ok_ws(ws, ws_bytes, n))
     return -1;
-  if (ngen > kMaxGen || (ngen && (!gen_masks || !slots || !d_grad))) return -1;
+  if (ngen > kMaxDiagGen || (ngen && (!gen_masks || !slots || !d_grad))) return -1;
   for (uint32_t t = 0; t < ngen; t++)
     if (n < 64 && (gen_masks[t] >> n)) return -1;
   if (!undo && ngen == 0) return 0;
@@ -445,10 +481,13 @@ extern "C" int qmk_adjoint_diagonal(float *psi, float *lam, uint32_t n, uint32_t
   if (ngen == 0)
     return launch_adj_diag<0>(psi, lam, n, dd, table, 0, nullptr, nullptr, nullptr, undo != 0, ws, s);
   // Up to 16 generators take the 16-slot kernel (an 8-slot one measured
-  // 15-25% slower on the same blocks), more the 32-slot one.
+  // 15-25% slower on the same blocks), up to 32 the 32-slot one, more the
+  // 48-slot one (MaxCut layers on 3-regular graphs of 22-32 vertices).
   if (ngen <= 16)
     return launch_adj_diag<16>(psi, lam, n, dd, table, ngen, gen_masks, slots, d_grad, undo != 0, ws, s);
-  return launch_adj_diag<32>(psi, lam, n, dd, table, ngen, gen_masks, slots, d_grad, undo != 0, ws, s);
+  if (ngen <= 32)
+    return launch_adj_diag<32>(psi, lam, n, dd, table, ngen, gen_masks, slots, d_grad, undo != 0, ws, s);
+  return launch_adj_diag<48>(psi, lam, n, dd, table, ngen, gen_masks, slots, d_grad, undo != 0, ws, s);
 }
 
 extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t nops,

@@ -11,6 +11,7 @@ namespace qmk_adj {
 using qmk::M2;
 
 constexpr int kMaxGen = 32;   // gradient slots one backward pass may write
+constexpr int kMaxDiagGen = 48;   // ... and one diagonal-block pass
 
 constexpr int kMaxWarpOps = 32;
 

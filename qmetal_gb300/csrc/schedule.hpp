@@ -120,8 +120,8 @@ struct BackwardStep {
   std::vector<size_t> gates;
 };
 
-// Generators per diagonal-block pass.
-constexpr uint32_t kDiagGensPerPass = 32;
+// Generators per diagonal-block pass (the kernel's largest slot count).
+constexpr uint32_t kDiagGensPerPass = 48;
 
 // The sweep from the final state back to the first parameterised block.
 // tile_high: wires >= 6 one window pass holds in registers (1..4).

@@ -172,3 +172,19 @@ def test_graph_mode_matches_the_loop():
     # a second batch reuses nothing from the first and still agrees
     again = run_mode(reqs, qm.BATCH_GRAPH, lanes=1)
     assert [x[0] for x in again] == [x[0] for x in graph]
+
+
+@pytest.mark.parametrize("n,count", [(10, None), (11, None), (14, 40), (16, 48), (13, 33)])
+def test_dense_cost_layers_against_the_oracle(n, count):
+    """Cost layers of 33 to 55 couplings: one 48-generator diagonal pass, or
+    48 and then the rest (the complete graph on 11 vertices)."""
+    rng = np.random.default_rng(n)
+    edges = [(a, b) for a in range(n) for b in range(a + 1, n)]
+    if count is not None:
+        edges = [edges[k] for k in sorted(rng.choice(len(edges), count, replace=False))]
+    gates = W.maxcut_qaoa(n, edges, rng.uniform(0, np.pi, 2), rng.uniform(0, np.pi, 2))
+    terms = W.maxcut_hamiltonian(edges)
+    e, g = qm.Simulator(n).energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    assert abs(e - e0) <= ETOL
+    assert np.abs(np.array(g) - g0).max() <= GTOL

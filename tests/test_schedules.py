@@ -268,7 +268,7 @@ def replay_backward(n, gates, terms, tile_high):
                 lam = apply_1q(lam, n, w, minv)
         elif s[0] == "diag":
             _, undo, tms, gphase, gens = s
-            assert len(gens) <= 32
+            assert len(gens) <= 48
             for z, slot in gens:
                 grad[slot] += np.vdot(lam, pauli_apply(psi, n, 0, 0, z)).imag
                 touched[slot] += 1
@@ -434,6 +434,23 @@ def test_backward_schedule_long_wire_and_tied():
     _, want = oracle.energy_and_gradient(n, gates, terms)
     assert np.abs(grad - want).max() < 1e-10
     assert sum(s[0] == "window" for s in steps) >= 3
+
+
+@pytest.mark.parametrize("n,split,undo", [(10, [45, 45], [True, False]),
+                                          (11, [48, 7, 48, 7], [False, True, False, False])])
+def test_backward_schedule_dense_cost_layer(n, split, undo):
+    """Cost layers on the complete graph: 45 couplings take one diagonal
+    pass, 55 a 48-generator pass and then the rest with the undo (none for
+    the first layer, where the sweep ends)."""
+    edges = [(a, b) for a in range(n) for b in range(a + 1, n)]
+    gates = W.maxcut_qaoa(n, edges, [0.4, 1.3], [0.7, 0.2])
+    terms = W.maxcut_hamiltonian(edges)
+    grad, touched, steps = replay_backward(n, gates, terms, 2)
+    _, want = oracle.energy_and_gradient(n, gates, terms)
+    assert np.abs(grad - want).max() < 1e-10
+    diag = [s for s in steps if s[0] == "diag" and s[4]]
+    assert [len(s[4]) for s in diag] == split
+    assert [bool(s[1]) for s in diag] == undo
 
 
 def test_schedule_export_errors():
