@@ -169,7 +169,7 @@ int qmk_zdiag_costate(float *lambda, const float *psi, uint32_t n, uint32_t num_
 
 /* Backward step over a whole diagonal block (terms as in
  * qmk_apply_diagonal, describing the block's forward phases): for each of the
- * ngen <= 32 Z-string generators, d_grad[slots[t]] = Im<lambda|Z_gen|psi>;
+ * ngen <= 48 Z-string generators, d_grad[slots[t]] = Im<lambda|Z_gen|psi>;
  * then, if undo, both states are multiplied by the conjugate phases, all in
  * one pass. Replaces the per-gate reduce_pauli2 and undo dispatches for the
  * block's RZ gates and ZZ couplings (kernels.metal:331-360;
