@@ -119,3 +119,25 @@ def test_wait_counter_sits_in_the_workspace_tail():
     assert take(ctypes.c_void_p(base), 16, ctypes.byref(out), None) == -1
     assert take(ctypes.c_void_p(base), ws_bytes, None, None) == -1
     assert out.value == 7
+
+
+def test_diagonal_adjoint_argument_limits_without_launching():
+    """At most 48 generators a pass, each inside the state's wires; both are
+    refused before anything reaches the device."""
+    lib = ctypes.CDLL(qm.library_path())
+    lib.qmk_workspace_bytes.restype = ctypes.c_size_t
+    lib.qmk_workspace_bytes.argtypes = [ctypes.c_uint32]
+    f = lib.qmk_adjoint_diagonal
+    f.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_double, ctypes.c_uint32,
+                  ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                  ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p]
+    n = 12
+    ws_bytes = lib.qmk_workspace_bytes(n)
+    fake = ctypes.c_void_p(1 << 20)          # never dereferenced: every call is refused
+    gens = (ctypes.c_uint64 * 49)(*([3] * 49))
+    slots = (ctypes.c_uint32 * 49)(*range(49))
+    assert f(fake, fake, n, 0, None, None, 0.0, 49, gens, slots, fake, 1, fake, ws_bytes, None) == -1
+    gens[47] = 1 << n                       # a generator outside the state's wires
+    assert f(fake, fake, n, 0, None, None, 0.0, 48, gens, slots, fake, 1, fake, ws_bytes, None) == -1
+    assert f(fake, fake, n, 0, None, None, 0.0, 48, None, slots, fake, 1, fake, ws_bytes, None) == -1
