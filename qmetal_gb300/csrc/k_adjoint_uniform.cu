@@ -75,8 +75,9 @@ __device__ __forceinline__ float split_one(float4 (&P)[kPairNV], float4 (&L)[kPa
 // Bulk copies through the TMA engine: one 512-byte row per instruction,
 // completion counted in bytes on a shared-memory mbarrier. Every wait is
 // bounded: a wait that gives up is counted in the workspace's wait counter
-// (Area::waits, read by the host after the pass) and the kernel goes on, so
-// it cannot hang.
+// (Area::waits, read by the host after the pass), the warp stops streaming
+// and drains its copies in flight before it exits, and the kernel goes on,
+// so it cannot hang.
 constexpr uint32_t kMaxWaitPolls = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -114,14 +115,12 @@ __device__ __forceinline__ void bulk_row(void *dst, const void *src, uint32_t by
 __device__ __forceinline__ void fence_proxy_async() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
-__device__ __forceinline__ void mbar_wait(uint64_t *mb, uint32_t parity, unsigned *gave_up) {
-  uint32_t polls = 0;
-  while (!mbar_try_wait(mb, parity)) {
-    if (++polls == kMaxWaitPolls) {
-      if ((threadIdx.x & 31) == 0) atomicAdd(gave_up, 1u);
-      break;
-    }
-  }
+// Bounded wait for a phase of the barrier; false if it gave up. Called by a
+// whole warp, which reduces the answer to one warp-uniform flag.
+__device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
+  for (uint32_t polls = 0; polls < kMaxWaitPolls; polls++)
+    if (mbar_try_wait(mb, parity)) return true;
+  return false;
 }
 
 // Four register wires on a warp pair (the fourth split across the pair),
@@ -173,6 +172,13 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   };
   __shared__ uint64_t mbar[kThreads / 32];   // one per warp: its next round's rows
   uint32_t parity = 0;
+  // A wait that gives up (counted in the workspace; the pass's results are
+  // then refused by the host) leaves one batch of copies in flight: the warp
+  // issues no more and waits for none (its slots' contents no longer
+  // matter), and before it exits waits once more, bounded, for that batch
+  // to land.
+  bool stalled = false;
+  uint32_t stalled_parity = 0;
   if constexpr (kPipe) {
     if (lane == 0) mbar_init(&mbar[warp], 1);
     fence_proxy_async();
@@ -181,7 +187,7 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   // The next round's rows of this warp (8 of each state), if it has one.
   auto prefetch = [&](uint64_t r) {
     const uint64_t ws = site(r);
-    if (r < rounds && ws < nwsites) {
+    if (r < rounds && ws < nwsites && !stalled) {
       const uint64_t row0 = base_of(ws) & ~31ull;
       __syncwarp();
       if (lane == 0) {
@@ -202,8 +208,13 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     const bool active = ws < nwsites;
     const uint64_t base = active ? base_of(ws) : 0;
     if constexpr (kPipe) {
-      if (active) {
-        mbar_wait(&mbar[warp], parity, a.waits);
+      if (active && !stalled) {
+        const bool landed = mbar_wait(&mbar[warp], parity);
+        if (!__all_sync(0xffffffffu, landed)) {
+          if (lane == 0) atomicAdd(a.waits, 1u);
+          stalled = true;
+          stalled_parity = parity;
+        }
         parity ^= 1u;
       }
     }
@@ -251,6 +262,10 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
         lam[v] = L[l];
       }
     }
+  }
+  if constexpr (kPipe) {
+    if (stalled && !__all_sync(0xffffffffu, mbar_wait(&mbar[warp], stalled_parity)) && lane == 0)
+      atomicAdd(a.waits, 1u);
   }
   double acc[NOPS];
 #pragma unroll
