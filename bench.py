@@ -15,7 +15,15 @@ in HBM; `e2e` repeats the step through the C ABI from host gate arrays
 (circuit build, reset, run, 1024 samples and the norm read back), wall-clock;
 `roofline` is the dominant kernel's achieved bandwidth from CUDA events around
 each op inside the timed region; `cpu_baseline` is the complex128 oracle on
-the host cores on a bounded sample (the same circuits at 20 qubits).
+the host cores on a bounded sample (the same fused plans at 20 qubits).
+
+Two more keys carry the other configurations of the metric, each measured in
+the same run after the timed region: `grad` (adjoint gradients of the HEA
+depth-8 problem at 28 and 33 qubits, block-wise and gate-by-gate sweeps on
+the same GPU, their difference, and the error against the complex128 oracle
+at 22 qubits) and `batch` (512 QAOA MaxCut requests served together, against
+the per-circuit loops, with the batch's roofline fraction and its error
+against the oracle).
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
@@ -39,12 +47,13 @@ sys.path.insert(0, ROOT)
 N_QUBITS = 30
 N_CPU = 20
 OP_NAMES = ["dense1q", "group", "blocked", "controlled1q", "diagonal", "swap", "ccx"]
-# DRAM bytes (read + write) per algorithmic byte of one launch, from the full
-# ncu captures at 26 qubits (profiles/group_diag_n26_full.md: k_group<4,0>
-# 536.9 + 475.8 MB, k_diag 537.0 + 477.4 MB against 2S = 1073.7 MB). The
-# traffic grows with the state, so a launch at n qubits moves this fraction
-# of its 2S.
+# DRAM bytes (read + write) per algorithmic byte of one launch, from ncu's
+# dram__bytes_read.sum + dram__bytes_write.sum on single launches at 26 qubits
+# (k_group<4,0>: 536.9 + 475.8 MB; k_diag: 537.0 + 477.4 MB; 2S = 1073.7 MB
+# each). The traffic grows with the state, so a launch at n qubits is charged
+# this fraction of its 2S.
 DRAM_PER_ALGO_BYTE = {1: (536.9 + 475.8) / 1073.7, 4: (537.0 + 477.4) / 1073.7}
+DRAM_CAPTURE_QUBITS = 26
 OP_STATE_PASSES = {0: 2.0, 1: 2.0, 2: 2.0, 3: 1.0, 4: 2.0, 5: 1.0, 6: 0.5}  # x S
 
 
@@ -172,34 +181,31 @@ def torch_sync():
         pass
 
 
-def cpu_oracle_run(n, gates):
+def cpu_sample(threads, copies=1, repeats=1, executor="plan"):
+    """The complex128 oracle (a restatement of the reference's CPU Reference)
+    on the workload's circuits at N_CPU qubits, one instance per thread,
+    `threads` instances concurrently. executor "plan" runs the fused plan op
+    by op (Reference::run(const Plan&), src/reference.cpp:208-248) -- the
+    same plans whose bytes are charged -- and "gates" the gate stream one gate
+    at a time. Returns (GB/s-equivalent, secs)."""
     import oracle
-    t0 = time.perf_counter()
-    oracle.run(n, gates)
-    return time.perf_counter() - t0
-
-
-def cpu_sample(threads, copies=1, repeats=1):
-    """The complex128 oracle (gate by gate, the reference's CPU algorithm) on
-    the workload's circuits at N_CPU qubits, each gate loop on one thread;
-    `threads` instances run concurrently. Returns (GB/s-equivalent, secs)."""
-    import oracle
-    import qmetal_gb300 as qm  # noqa: F401  (plan kinds come from the library)
+    import qmetal_gb300 as qm  # noqa: F401  (plans come from the library)
     from qmetal_gb300 import workloads as W
     oracle.set_threads(1)
     jobs, total_bytes = [], 0.0
     for _name, gates in workload(N_CPU):
-        kinds = plan_kinds(W.to_circuit(N_CPU, gates).plan_export())
+        plan = W.to_circuit(N_CPU, gates).plan_export()
         for _ in range(copies * repeats):
-            jobs.append(gates)
-            total_bytes += circuit_bytes(kinds, N_CPU)
+            jobs.append(plan if executor == "plan" else gates)
+            total_bytes += circuit_bytes(plan_kinds(plan), N_CPU)
+    run = oracle.run_plan if executor == "plan" else oracle.run
     t0 = time.perf_counter()
     if threads == 1:
-        for g in jobs:
-            cpu_oracle_run(N_CPU, g)
+        for job in jobs:
+            run(N_CPU, job)
     else:
         with cf.ThreadPoolExecutor(max_workers=threads) as ex:
-            list(ex.map(lambda g: cpu_oracle_run(N_CPU, g), jobs))
+            list(ex.map(lambda job: run(N_CPU, job), jobs))
     dt = time.perf_counter() - t0
     return total_bytes / dt / 1e9, dt
 
@@ -207,8 +213,9 @@ def cpu_sample(threads, copies=1, repeats=1):
 def run_reference(args, world, rank, dist):
     """The reference's CPU implementation of the path (the oracle port of its
     complex128 Reference; its own sources are not on this machine), all host
-    threads, each step a bounded sample: every workload circuit at N_CPU
-    qubits, cores/4 copies of each run concurrently."""
+    threads, each step a bounded sample: every workload circuit's fused plan at
+    N_CPU qubits executed op by op, cores/4 copies of each run concurrently.
+    The gate-by-gate form of the same circuits is timed once beside it."""
     if rank != 0:
         return
     import oracle
@@ -223,63 +230,169 @@ def run_reference(args, world, rank, dist):
         rates.append(r)
         secs += dt
     value = args.steps / sum(1.0 / r for r in rates)   # total bytes / total time
+    gbg_rate, gbg_secs = cpu_sample(threads, copies, executor="gates")
     kind = "reference" if oracle.ref_available() else "port"
     line = {
         "impl": "reference", "metric": "fused_plan_hbm_gbs", "value": round(value, 3),
         "unit": "GB/s", "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(1e3 * secs / args.steps, 3), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "c128", "data": "synthetic",
-        "config": {"workload": f"fused-plan circuits of the 30-qubit config, run at {N_CPU} "
+        "config": {"workload": f"fused plans of the 30-qubit config, run at {N_CPU} "
                                "qubits on the host (bounded sample)",
                    "num_qubits": N_CPU, "circuits": [c for c, _ in workload(4)],
                    "copies_per_circuit": copies},
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": threads,
                          "kind": kind,
-                         "sample": f"4 circuits x {copies} copies at n={N_CPU}, complex128, "
-                                   f"gate by gate, {threads} threads"},
+                         "sample": f"4 fused plans x {copies} copies at n={N_CPU}, complex128, "
+                                   f"plan op by op, {threads} threads"},
+        "gate_by_gate": {"value": round(gbg_rate, 3), "unit": "GB/s",
+                         "seconds": round(gbg_secs, 3),
+                         "what": "the same circuits gate by gate (no fusion), same bytes charged"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
 
 
-def run_batch_workload(args, world, rank, dist):
+# --- algorithmic bytes of one serving request -------------------------------
+# Each launch is charged 16 B per amplitude it must read and write, as the
+# plan ops are: a one-qubit group pass or a permutation pass 2S, a window-tile
+# or diagonal-block undo pass over both states 4S (a diagonal block without
+# its undo 2S), one gate undone on both states twice that gate's bytes, the
+# co-state passes 2S (written from psi) or 3S (accumulated), the energy dot
+# product 2S, the |0> reset S and the sampler's block sums S.
+GATE_STATE_PASSES = {12: 1.0, 13: 1.0, 14: 0.5, 15: 1.0, 16: 0.5, 17: 0.5}  # else 2S
+
+
+def _forward_bytes(flat, plan_kinds_, S):
+    total, pos = 0.0, 1
+    for _ in range(int(flat[0])):
+        kind = int(flat[pos])
+        if kind == 0:
+            nw = int(flat[pos + 1])
+            total += 2 * S
+            pos += 2 + 9 * nw
+        elif kind == 1:
+            n = int(flat[pos + 1])
+            nops = int(flat[pos + 3 + n])
+            total += 2 * S
+            pos += 4 + n + nops
+        else:
+            total += OP_STATE_PASSES[plan_kinds_[int(flat[pos + 1])]] * S
+            pos += 2
+    assert pos == len(flat), "schedule layout"
+    return total
+
+
+def _costate_bytes(flat, S):
+    total, pos = 0.0, 1
+    for _ in range(int(flat[0])):
+        kind = int(flat[pos])
+        if kind == 0:
+            nt = int(flat[pos + 1])
+            total += 2 * S
+            pos += 2 + 2 * nt
+        elif kind == 1:
+            overwrite, nt = int(flat[pos + 1]), int(flat[pos + 2])
+            total += (2 if overwrite else 3) * S
+            pos += 3 + 4 * nt
+        elif kind == 2:
+            overwrite, nt = int(flat[pos + 1]), int(flat[pos + 3])
+            total += (2 if overwrite else 3) * S
+            pos += 4 + 3 * nt
+        else:
+            total += (1 if kind == 3 else 2) * S
+            pos += 1
+    assert pos == len(flat), "schedule layout"
+    return total
+
+
+def _backward_bytes(flat, gates, S):
+    total, pos = 0.0, 1
+    for _ in range(int(flat[0])):
+        kind = int(flat[pos])
+        if kind == 0:
+            nops = int(flat[pos + 1])
+            total += 4 * S
+            pos += 2 + 11 * nops
+        elif kind == 1:
+            undo, nt = int(flat[pos + 1]), int(flat[pos + 2])
+            ng = int(flat[pos + 4 + 2 * nt])
+            total += (4 if undo else 2) * S
+            pos += 5 + 2 * nt + 2 * ng
+        elif kind == 2:
+            n = int(flat[pos + 1])
+            ng = int(flat[pos + 3 + n])
+            total += 4 * S
+            pos += 4 + n + ng
+        else:
+            k = gates[int(flat[pos + 1])][0]
+            total += 2 * GATE_STATE_PASSES.get(k, 2.0) * S
+            pos += 2
+    assert pos == len(flat), "schedule layout"
+    return total
+
+
+def request_bytes(n, gates, circuit, hamiltonian, shots, tile_high):
+    """Algorithmic HBM bytes of one request served by Simulator::serve:
+    reset, merged forward, samples, co-state and energy, block-wise sweep."""
+    S = 8.0 * (1 << n)
+    kinds = plan_kinds(circuit.plan_export())
+    total = S + _forward_bytes(circuit.schedule_export("forward"), kinds, S)
+    if shots:
+        total += S
+    total += _costate_bytes(circuit.schedule_export("costate", hamiltonian), S)
+    total += _backward_bytes(circuit.schedule_export("backward", tile_high=tile_high), gates, S)
+    return total
+
+
+def batch_results(requests=512, steps=3, warmup=3, lanes=0, widths=None, loops=True,
+                  oracle_max_n=16, dist=None, world=1, rank=0):
     """512 QAOA MaxCut requests (n uniform over the even widths 12..26, p in
     1..8, random 3-regular graphs, angles ~ U[0, pi]), each energy + adjoint
     gradient + 4096 samples. A step serves the whole batch with concurrent
-    lanes; the per-circuit loop a caller of the reference API would write
-    (gate-by-gate gradient, run, sample) is timed once beside it, and so is
-    the loop with the block-wise gradient. Wall clock, host buffers."""
+    lanes (wall clock, host buffers). Beside it, once each: the same batch as
+    one CUDA graph, the per-circuit loop with the same block-wise sweep, and
+    the per-circuit loop a caller of the reference API would write
+    (gate-by-gate gradient, run, sample). Returns a dict."""
     import numpy as np
     import qmetal_gb300 as qm
     from qmetal_gb300 import workloads as W
-    insts = W.maxcut_instances(args.requests, seed=6)
-    if args.widths:
-        insts = [i for i in insts if i["n"] in args.widths]
-    reqs = []
+    insts = W.maxcut_instances(requests, seed=6)
+    if widths:
+        insts = [i for i in insts if i["n"] in widths]
+    reqs, streams = [], []
     for k, inst in enumerate(insts):
         gates = W.maxcut_qaoa(inst["n"], inst["edges"], inst["gammas"], inst["betas"])
         reqs.append((W.to_circuit(inst["n"], gates),
                      W.to_hamiltonian(W.maxcut_hamiltonian(inst["edges"])), 4096, 7000 + k))
+        streams.append(gates)
     params = sum(len(c) for c, _h, _s, _seed in reqs)
 
-    tuning = qm.batch_autotune(reqs) if args.lanes == 0 else None
+    tuning = qm.batch_autotune(reqs) if lanes == 0 else None
+    tile_of = (tuning or {}).get("tile_high", {})
+    batch_bytes = sum(request_bytes(c.num_qubits, g, c, h, s, tile_of.get(c.num_qubits, 4))
+                      for (c, h, s, _seed), g in zip(reqs, streams))
+    h2d = sum(sum(4 + 4 * len(q) + 8 * len(p) for _k, q, p in g) for g in streams)
+    d2h = sum(8 + 8 * len(c) + 8 * s for c, _h, s, _seed in reqs)
 
     def serve(mode):
         torch_sync()
         t0 = time.perf_counter()
-        out = qm.batch_serve(reqs, mode=mode, lanes=args.lanes)
+        out = qm.batch_serve(reqs, mode=mode, lanes=lanes)
         return out, time.perf_counter() - t0
 
-    for _ in range(max(args.warmup, 3)):
+    for _ in range(max(warmup, 3)):
         serve(qm.BATCH_LANES)
     barrier(dist, world)
     with ClockSampler(0 if world == 1 else int(os.environ.get("LOCAL_RANK", "0"))) as clocks:
         times = []
-        for _ in range(args.steps):
+        for _ in range(steps):
             lanes_out, dt = serve(qm.BATCH_LANES)
             times.append(dt)
     wall = max_over_ranks(sum(times), dist, world)
+    per_batch = wall / steps
+    peak, peak_src = peaks()
     # The same batch recorded into one CUDA graph and launched once (tile
     # shapes from the tuning above); wall clock includes recording.
     graph_runs = []
@@ -289,127 +402,151 @@ def run_batch_workload(args, world, rank, dist):
     graph_t, graph_timing = min(graph_runs, key=lambda r: r[0])
     graph_diff = max(float(np.max(np.abs(np.array(a[1]) - np.array(b[1])))) for a, b in
                      zip(lanes_out, graph_out))
-    if args.no_loops:
-        plain_out, plain_t = lanes_out, float("nan")
-        fused_out, fused_t = lanes_out, float("nan")
-    else:
-        plain_out, plain_t = serve(qm.BATCH_PLAIN_LOOP)
+    out = {
+        "value": round(len(reqs) / per_batch, 2), "unit": "requests/s",
+        "s_per_batch": round(per_batch, 4), "steps": steps, "warmup": max(warmup, 3),
+        "requests": len(reqs), "widths": sorted({i["n"] for i in insts}), "gate_params": params,
+        "lanes": tuning["lanes"] if tuning else lanes, "autotuned": tuning,
+        "roofline": {"bound": "hbm", "algorithmic_bytes_per_batch": batch_bytes,
+                     "achieved": round(batch_bytes / per_batch / 1e9, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(batch_bytes / per_batch / 1e9 / peak, 4),
+                     "peak_source": peak_src,
+                     "what": "every launch's algorithmic bytes summed over the batch, over "
+                             "the batch's wall-clock time (host buffers, all lanes)"},
+        "e2e": {"value": round(len(reqs) / per_batch, 2), "unit": "requests/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "graph": {"value": round(len(reqs) / graph_t, 2), "unit": "requests/s",
+                  "seconds": round(graph_t, 3),
+                  "record_s": round(graph_timing["record_s"], 3),
+                  "instantiate_s": round(graph_timing["instantiate_s"], 3),
+                  "execute_s": round(graph_timing["execute_s"], 3),
+                  "nodes": graph_timing["nodes"], "max_grad_diff_vs_lanes": graph_diff,
+                  "what": "every request recorded into one CUDA graph, one launch"},
+        "clocks": clocks.summary(),
+    }
+    if loops:
         fused_out, fused_t = serve(qm.BATCH_FUSED_LOOP)
-    gdiff = max(float(np.max(np.abs(np.array(a[1]) - np.array(b[1])))) for a, b in
-                zip(lanes_out, plain_out))
-    ediff = max(abs(a[0] - b[0]) for a, b in zip(lanes_out, plain_out))
-    oracle_err = None
-    if rank == 0 and not args.no_loops:
+        plain_out, plain_t = serve(qm.BATCH_PLAIN_LOOP)
+        out["blockwise_loop"] = {
+            "value": round(len(reqs) / fused_t, 2), "unit": "requests/s",
+            "seconds": round(fused_t, 3),
+            "what": "per-circuit loop with the same block-wise sweep, one request at a time"}
+        out["plain_loop"] = {
+            "value": round(len(reqs) / plain_t, 2), "unit": "requests/s",
+            "seconds": round(plain_t, 3),
+            "what": "per-circuit loop as a caller of the reference API writes it: "
+                    "gate-by-gate adjoint, run, sample"}
+        out["speedup_vs_blockwise_loop"] = round(fused_t / per_batch, 3)
+        out["speedup_vs_plain_loop"] = round(plain_t / per_batch, 2)
+        out["max_grad_diff_vs_plain"] = max(
+            float(np.max(np.abs(np.array(a[1]) - np.array(b[1]))))
+            for a, b in zip(lanes_out, plain_out))
+        out["max_energy_diff_vs_plain"] = max(abs(a[0] - b[0])
+                                              for a, b in zip(lanes_out, plain_out))
+    if rank == 0 and oracle_max_n:
         import oracle
         oracle.build()
-        e_worst = g_worst = g_rel = 0.0
+        e_worst = e_rel = g_worst = g_rel = 0.0
         checked = 0
-        for (c, _h, _s, _seed), inst, got in zip(reqs, insts, lanes_out):
-            if inst["n"] > 16:
+        for inst, gates, got in zip(insts, streams, lanes_out):
+            if inst["n"] > oracle_max_n:
                 continue
-            gates = W.maxcut_qaoa(inst["n"], inst["edges"], inst["gammas"], inst["betas"])
             e0, g0 = oracle.energy_and_gradient(inst["n"], gates,
                                                 W.maxcut_hamiltonian(inst["edges"]))
             gd = float(np.max(np.abs(np.array(got[1]) - g0)))
             e_worst = max(e_worst, abs(got[0] - e0))
+            e_rel = max(e_rel, abs(got[0] - e0) / max(abs(e0), 1e-30))
             g_worst = max(g_worst, gd)
             g_rel = max(g_rel, gd / max(float(np.max(np.abs(g0))), 1e-30))
             checked += 1
-        oracle_err = {"requests_checked": checked, "widths": "n <= 16",
-                      "max_abs_energy_err": e_worst, "max_abs_grad_err": g_worst,
-                      "max_grad_err_rel_to_max_grad": g_rel}
-    value = world * args.steps * len(reqs) / wall
+        out["err_vs_complex128_oracle"] = {
+            "requests_checked": checked, "widths": f"n <= {oracle_max_n}",
+            "max_abs_energy_err": e_worst, "max_rel_energy_err": e_rel,
+            "max_abs_grad_err": g_worst, "max_grad_err_rel_to_max_grad": g_rel}
+    return out
+
+
+def run_batch_workload(args, world, rank, dist):
+    """The batched-serving configuration as its own line (see batch_results)."""
+    r = batch_results(args.requests, args.steps, args.warmup, args.lanes, args.widths,
+                      loops=not args.no_loops, oracle_max_n=0 if args.no_loops else 16,
+                      dist=dist, world=world, rank=rank)
     if rank == 0:
-        widths = sorted({i["n"] for i in insts})
         line = {
-            "metric": "batched_adjoint_requests_per_s", "value": round(value, 2),
+            "metric": "batched_adjoint_requests_per_s", "value": round(world * r["value"], 2),
             "unit": "requests/s", "n_gpus": world, "steps": args.steps,
-            "warmup": max(args.warmup, 3), "ms_per_step": round(1e3 * wall / args.steps, 2),
+            "warmup": r["warmup"], "ms_per_step": round(1e3 * r["s_per_batch"], 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64",
             "data": "synthetic",
-            "config": {"workload": f"{len(reqs)} QAOA MaxCut requests (energy + adjoint "
+            "config": {"workload": f"{r['requests']} QAOA MaxCut requests (energy + adjoint "
                                    "gradient + 4096 samples each)",
-                       "widths": widths, "gate_params": params,
-                       "lanes": tuning["lanes"] if tuning else args.lanes,
-                       "autotuned": tuning},
-            "plain_loop": {"value": round(len(reqs) / plain_t, 2), "unit": "requests/s",
-                           "seconds": round(plain_t, 3),
-                           "what": "per-circuit loop: gate-by-gate adjoint, run, sample"},
-            "blockwise_loop": {"value": round(len(reqs) / fused_t, 2), "unit": "requests/s",
-                               "seconds": round(fused_t, 3)},
-            "graph": {"value": round(len(reqs) / graph_t, 2), "unit": "requests/s",
-                      "seconds": round(graph_t, 3),
-                      "record_s": round(graph_timing["record_s"], 3),
-                      "instantiate_s": round(graph_timing["instantiate_s"], 3),
-                      "execute_s": round(graph_timing["execute_s"], 3),
-                      "nodes": graph_timing["nodes"],
-                      "max_grad_diff_vs_lanes": graph_diff,
-                      "what": "every request recorded into one CUDA graph, one launch"},
-            "speedup_vs_plain_loop": round(plain_t / (wall / args.steps), 2),
-            "max_grad_diff_vs_plain": gdiff, "max_energy_diff_vs_plain": ediff,
-            "err_vs_complex128_oracle": oracle_err,
-            "clocks": clocks.summary(),
+                       "widths": r["widths"], "gate_params": r["gate_params"],
+                       "lanes": r["lanes"], "autotuned": r["autotuned"]},
+            **{k: v for k, v in r.items() if k not in ("value", "unit", "steps", "warmup")},
         }
-        if args.no_loops:
-            for key in ("plain_loop", "blockwise_loop", "speedup_vs_plain_loop",
-                        "max_grad_diff_vs_plain", "max_energy_diff_vs_plain"):
-                line[key] = None
         print(json.dumps(line), flush=True)
     barrier(dist, world)
 
 
-def run_grad_workload(args, world, rank, dist):
+def grad_results(qubits, reps=5, gate_by_gate=True, oracle_qubits=22):
     """Adjoint gradients of the HEA depth-8 problem (RY + RZ per wire per
-    layer, CX ladder; H = -sum Z_i Z_{i+1} - 0.7 sum X_i on a ring) at 28 and
-    33 qubits: device time per gradient with the block-wise sweep (the
-    default) and with the reference's gate-by-gate sweep, and a central
-    difference check (eps = 1e-3) on a few parameters."""
+    layer, CX ladder; H = -sum Z_i Z_{i+1} - 0.7 sum X_i on a ring): device
+    seconds per gradient with the block-wise sweep (the default) and with the
+    reference's gate-by-gate sweep on the same GPU, the largest difference
+    between the two gradients at each width, and, at oracle_qubits, every
+    entry against the complex128 oracle's adjoint gradient."""
     import numpy as np
     import qmetal_gb300 as qm
     from qmetal_gb300 import workloads as W
     results = {}
-    for n in args.grad_qubits:
+    for n in qubits:
         gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
         c, h = W.to_circuit(n, gates), W.to_hamiltonian(terms)
         nparams = sum(1 for g in gates if g[2])
         sim = qm.Simulator(n)
         entry = {"gates": len(gates), "params": nparams}
-        modes = (("blockwise", True),) if args.no_loops else \
-            (("blockwise", True), ("gate_by_gate", False))
-        for label, fused in modes:
-            sim.energy_and_gradient(c, h, fused=fused)      # warm-up
+        sim.energy_and_gradient(c, h)      # warm-up (first use takes the co-state)
+        sim.elapsed()
+        for _ in range(reps):
+            e, g = sim.energy_and_gradient(c, h)
+        t = sim.elapsed() / reps
+        entry["blockwise"] = {"s_per_gradient": round(t, 4), "grad_per_s": round(1.0 / t, 3),
+                              "param_grads_per_s": round(nparams / t, 1), "reps": reps}
+        entry["energy"] = e
+        if gate_by_gate:
             sim.elapsed()
-            reps = args.steps if fused else 1
-            for _ in range(reps):
-                e, g = sim.energy_and_gradient(c, h, fused=fused)
-            t = sim.elapsed() / reps
-            entry[label] = {"s_per_gradient": round(t, 4), "grad_per_s": round(1.0 / t, 3),
-                            "param_grads_per_s": round(nparams / t, 1)}
-            entry.setdefault("energy", e)
-            entry.setdefault("_grad", g)
-        g = entry.pop("_grad")
-        if args.no_loops:
-            results[f"n{n}"] = entry
-            sim.close()
-            del sim
-            continue
-        entry["speedup"] = round(entry["gate_by_gate"]["s_per_gradient"]
-                                 / entry["blockwise"]["s_per_gradient"], 2)
-        worst = 0.0
-        eps = 1e-3
-        for j in (0, len(gates) // 2, len(gates) - n - 2):
-            while not gates[j][2]:
-                j += 1
-            kind, qs, ps = gates[j]
-            plus = list(gates); plus[j] = (kind, qs, (ps[0] + eps,))
-            minus = list(gates); minus[j] = (kind, qs, (ps[0] - eps,))
-            sim.reset(); sim.run(W.to_circuit(n, plus)); ep = sim.expectation(h)
-            sim.reset(); sim.run(W.to_circuit(n, minus)); em = sim.expectation(h)
-            worst = max(worst, abs((ep - em) / (2 * eps) - g[j]))
-        entry["max_abs_diff_vs_central_difference"] = worst
+            e1, g1 = sim.energy_and_gradient(c, h, fused=False)
+            t1 = sim.elapsed()
+            entry["gate_by_gate"] = {"s_per_gradient": round(t1, 4),
+                                     "grad_per_s": round(1.0 / t1, 3),
+                                     "param_grads_per_s": round(nparams / t1, 1), "reps": 1}
+            entry["speedup"] = round(t1 / t, 2)
+            entry["max_abs_grad_diff_vs_gate_by_gate"] = float(
+                np.max(np.abs(np.array(g) - np.array(g1))))
+            entry["abs_energy_diff_vs_gate_by_gate"] = abs(e - e1)
         results[f"n{n}"] = entry
         sim.close()
         del sim
+    if oracle_qubits:
+        import oracle
+        oracle.build()
+        n = oracle_qubits
+        gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
+        sim = qm.Simulator(n)
+        e, g = sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+        sim.close()
+        e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+        results["err_vs_complex128_oracle"] = {
+            "n": n, "params": sum(1 for x in gates if x[2]),
+            "max_abs_grad_err": float(np.max(np.abs(np.array(g) - g0))),
+            "abs_energy_err": abs(e - e0)}
+    return results
+
+
+def run_grad_workload(args, world, rank, dist):
+    """The gradient configuration as its own line (see grad_results)."""
+    results = grad_results(args.grad_qubits, args.steps, gate_by_gate=not args.no_loops,
+                           oracle_qubits=0 if args.no_loops else 22)
     if rank == 0:
         first = results[f"n{args.grad_qubits[0]}"]
         line = {
@@ -579,6 +716,14 @@ def main():
     ap.add_argument("--block-bits", type=int, default=10,
                     help="ablation: cache-blocking window, log2 amplitudes")
     ap.add_argument("--grad-qubits", type=int, nargs="+", default=[28, 33])
+    ap.add_argument("--grad-reps", type=int, default=3,
+                    help="timed block-wise gradients per width in the default run's grad key")
+    ap.add_argument("--batch-steps", type=int, default=3,
+                    help="timed batches in the default run's batch key")
+    ap.add_argument("--no-grad", action="store_true",
+                    help="default run: leave out the gradient configuration (grad key)")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="default run: leave out the batched-serving configuration (batch key)")
     ap.add_argument("--requests", type=int, default=512)
     ap.add_argument("--lanes", type=int, default=0,
                     help="batch lanes; 0 = autotuned on the batch's own requests")
@@ -748,6 +893,16 @@ def main():
             big.close()
             del big
 
+    # --- the gradient and batched-serving configurations, as sub-keys -------
+    grad = None
+    if not args.no_grad:
+        grad = grad_results(args.grad_qubits, reps=args.grad_reps, gate_by_gate=True,
+                            oracle_qubits=22)
+    batch = None
+    if not args.no_batch:
+        batch = batch_results(args.requests, steps=args.batch_steps, warmup=3, lanes=args.lanes,
+                              loops=True, oracle_max_n=16, dist=dist, world=world, rank=rank)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         import oracle
@@ -755,8 +910,8 @@ def main():
         rate, secs = cpu_sample(1, repeats=3)
         cpu = {"value": round(rate, 4), "unit": "GB/s", "cores": 1,
                "kind": "reference" if oracle.ref_available() else "port",
-               "sample": f"the 4 circuits 3 times at n={N_CPU}, complex128 gate by gate, "
-                         f"1 thread, {secs:.1f} s"}
+               "sample": f"the 4 fused plans 3 times at n={N_CPU}, complex128, plan op by "
+                         f"op, 1 thread, {secs:.1f} s"}
 
     if rank == 0:
         ops_per_circuit = [len(k) for k in kinds]
@@ -779,8 +934,9 @@ def main():
                          "peak_source": peak_src,
                          "traffic": (round(DRAM_PER_ALGO_BYTE[dom] * op_bytes(dom, n))
                                      if dom in DRAM_PER_ALGO_BYTE else None),
-                         "traffic_source": "ncu dram bytes per launch at n=26, scaled by "
-                                           "units to this n"},
+                         "traffic_source": f"ncu dram bytes per launch at "
+                                           f"n={DRAM_CAPTURE_QUBITS}, scaled by units to "
+                                           f"n={n}"},
             "kernels": breakdown,
             "frac_of_peak_overall": round(value / world / peak, 4),
             "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
@@ -793,6 +949,8 @@ def main():
             "merged": {"s_per_circuit": round(merged_s, 5),
                        "speedup_vs_plan": round(dev_max / args.steps / len(circuits) / merged_s, 3),
                        "circuits": merged},
+            "grad": grad,
+            "batch": batch,
         }
         print(json.dumps(line), flush=True)
     barrier(dist, world)

@@ -202,6 +202,13 @@ int qm_energy_and_gradient_mode(qm_simulator s, qm_circuit c,
                                 const qm_hamiltonian *h, int mode,
                                 double *out_energy, double *out_grad);
 
+/* Fault injection for tests of the fail-closed path: the bounded bulk-copy
+ * waits inside this simulator's adjoint window passes give up after `polls`
+ * polls (0: at once); a negative value restores the full bound. A gradient
+ * whose pass gave up a wait returns -1 with "a bulk-copy wait timed out" in
+ * qm_last_error() and leaves the state reset to |0...0>. */
+int qm_set_wait_poll_limit(qm_simulator s, int64_t polls);
+
 /* One serving request of a batch: the circuit's width is its qubit count. */
 typedef struct {
   qm_circuit circuit;

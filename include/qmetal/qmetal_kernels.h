@@ -102,9 +102,11 @@ int qmk_apply_diagonal(float *state, uint32_t n, uint32_t num_terms,
  * loading this library holds until the process exits. Allocates nothing
  * (no cudaMalloc / cudaFree or any allocating routine). The first call on
  * each device looks up the array's device address (cudaGetSymbolAddress),
- * so make that first call before any stream capture. All calls share the
- * array: calls whose kernels may overlap on the GPU race. States above 34
- * qubits return QMK_ERR_TOO_LARGE. */
+ * so make that first call before any stream capture. The address is kept
+ * for the life of the process, so do not call this again on a device after
+ * cudaDeviceReset in the same process (the reset drops the array with the
+ * context). All calls share the array: calls whose kernels may overlap on
+ * the GPU race. States above 34 qubits return QMK_ERR_TOO_LARGE. */
 int qmk_apply_diagonal_noalloc(float *state, uint32_t n, uint32_t num_terms,
                                const uint64_t *masks, const double *angles,
                                double global_phase, void *stream);
@@ -208,6 +210,16 @@ int qmk_take_wait_timeouts(void *workspace, size_t workspace_bytes, unsigned int
  * qmk_workspace_init zeroes and the passes only increase), for a caller that
  * reads it with its own asynchronous copy. */
 unsigned int *qmk_wait_counter(void *workspace);
+
+/* Fault injection for tests: the bounded bulk-copy waits inside the window
+ * passes that run on `workspace` give up after `polls` polls (0: at once,
+ * so the pass is counted as timed out and its results are invalid); a
+ * negative value restores the full bound (2^22 polls). The wait each block
+ * makes before it exits, for copies still in flight, always keeps the full
+ * bound. Ordered on `stream`, which it synchronises. 0, -1 (bad arguments)
+ * or a CUDA error code. */
+int qmk_set_wait_poll_limit(void *workspace, size_t workspace_bytes, long long polls,
+                            void *stream);
 
 /* Sampling workspace bytes for n qubits (block CDF in FP64). */
 size_t qmk_sample_workspace_bytes(uint32_t n);

@@ -31,7 +31,6 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libqoracle.so")
 REF_LIB = os.path.join(HERE, "_ref", "libqref.so")
-REF_SOURCES = "/root/reference"
 
 _d, _u32, _u64, _i32 = POINTER(c_double), POINTER(c_uint32), POINTER(c_uint64), POINTER(c_int32)
 
@@ -49,12 +48,28 @@ def build() -> str:
     return LIB
 
 
+_where = None
+
+
+def reference_sources() -> str | None:
+    """The reference project's source tree, where this machine has one (the
+    recipe build_ref.sh decides: QMETAL_REFERENCE_SRC, else its default), or
+    None."""
+    global _where
+    if _where is None:
+        r = subprocess.run(["sh", os.path.join(HERE, "build_ref.sh"), "--where"],
+                           capture_output=True, text=True)
+        _where = r.stdout.strip() if r.returncode == 0 else ""
+    return _where or None
+
+
 def build_ref() -> str | None:
     """Compile the reference's own CPU code when its sources are present."""
-    if not os.path.exists(os.path.join(REF_SOURCES, "src", "reference.cpp")):
+    src = reference_sources()
+    if src is None:
         return None
     script = os.path.join(HERE, "build_ref.sh")
-    subprocess.run(["sh", script], check=True, env=dict(os.environ, REF=REF_SOURCES),
+    subprocess.run(["sh", script], check=True, env=dict(os.environ, QMETAL_REFERENCE_SRC=src),
                    capture_output=True)
     return REF_LIB
 

@@ -129,6 +129,7 @@ _energy_grad = _decl("qm_energy_and_gradient", c_int, c_void_p, c_void_p,
 _energy_grad_mode = _decl("qm_energy_and_gradient_mode", c_int, c_void_p, c_void_p,
                           POINTER(_Hamiltonian), c_int, _f64p, _f64p)
 _elapsed = _decl("qm_elapsed", c_int, c_void_p, _f64p)
+_wait_poll_limit = _decl("qm_set_wait_poll_limit", c_int, c_void_p, ctypes.c_int64)
 
 
 class _BatchItem(ctypes.Structure):
@@ -456,6 +457,13 @@ class Simulator:
         else:
             _check(_energy_grad_mode(self._h, circuit._h, byref(h), 1, byref(energy), grad))
         return energy.value, list(grad)[:len(circuit)]
+
+    def set_wait_poll_limit(self, polls: int):
+        """Fault injection for tests: the adjoint window passes' bounded
+        bulk-copy waits give up after `polls` polls (0: at once), so the next
+        gradient fails closed; a negative value restores the full bound."""
+        _check(_wait_poll_limit(self._h, int(polls)))
+        return self
 
     def run_profiled(self, circuit: Circuit, fuse: bool = True):
         """Run with a CUDA event between plan ops; returns each op's device

@@ -433,6 +433,14 @@ int qm_run_profiled(qm_simulator s, qm_circuit c, int fuse, double *out, size_t 
   });
 }
 
+int qm_set_wait_poll_limit(qm_simulator s, int64_t polls) {
+  if (!s) {
+    set_error("null argument");
+    return -1;
+  }
+  return guarded([&] { s->s->set_wait_poll_limit(static_cast<long long>(polls)); });
+}
+
 int qm_energy_and_gradient_mode(qm_simulator s, qm_circuit c, const qm_hamiltonian *h, int mode,
                                 double *out_energy, double *out_grad) {
   if (!s || !c || !h || !out_grad) {

@@ -82,6 +82,45 @@ uint32_t PauliString::weight() const {
   return uint32_t(__builtin_popcountll(x_mask | y_mask | z_mask));
 }
 
+PauliString PauliString::parse(const std::string &s) {
+  if (s.size() > 64) throw std::runtime_error("PauliString::parse: more than 64 qubits");
+  PauliString p;
+  for (size_t q = 0; q < s.size(); q++) {
+    const uint64_t bit = 1ull << q;
+    switch (s[q]) {
+      case 'I': case 'i': break;
+      case 'X': case 'x': p.x_mask |= bit; break;
+      case 'Y': case 'y': p.y_mask |= bit; break;
+      case 'Z': case 'z': p.z_mask |= bit; break;
+      default: throw std::runtime_error(std::string("PauliString::parse: bad character '") + s[q] + "'");
+    }
+  }
+  return p;
+}
+
+std::string PauliString::to_string(uint32_t n) const {
+  std::string out(n, 'I');
+  for (uint32_t q = 0; q < n && q < 64; q++) {
+    const uint64_t bit = 1ull << q;
+    if (x_mask & bit) out[q] = 'X';
+    else if (y_mask & bit) out[q] = 'Y';
+    else if (z_mask & bit) out[q] = 'Z';
+  }
+  return out;
+}
+
+size_t Circuit::count_1q() const {
+  size_t k = 0;
+  for (const Gate &g : ops) k += g.num_qubits == 1;
+  return k;
+}
+
+size_t Circuit::count_2q() const {
+  size_t k = 0;
+  for (const Gate &g : ops) k += g.num_qubits == 2;
+  return k;
+}
+
 PauliString PauliString::single(char axis, uint32_t q) {
   PauliString p;
   const uint64_t bit = 1ull << q;

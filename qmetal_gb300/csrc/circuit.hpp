@@ -47,6 +47,8 @@ struct Circuit {
   std::vector<Gate> ops;
   void add(const Gate &g) { ops.push_back(g); }
   size_t size() const { return ops.size(); }
+  size_t count_1q() const;   // gates by arity
+  size_t count_2q() const;
 };
 
 const char *gate_name(GateKind k);
@@ -58,6 +60,10 @@ struct PauliString {
   uint64_t x_mask = 0, y_mask = 0, z_mask = 0;
   bool valid(uint32_t num_qubits) const;
   uint32_t weight() const;
+  // "IXYZ" text, qubit 0 first (at most 64 characters); throws on anything else.
+  static PauliString parse(const std::string &s);
+  std::string to_string(uint32_t num_qubits) const;
+  static PauliString identity() { return PauliString{}; }
   static PauliString single(char axis, uint32_t q);
 };
 
@@ -88,6 +94,7 @@ struct PlanOp {
   std::vector<uint32_t> group_qubits;
   std::vector<cdouble> group_matrices;
   uint32_t block_bits = 0;
+  size_t term_count() const { return masks.size(); }
 };
 
 struct Plan {
@@ -103,6 +110,11 @@ struct FusionOptions {
   uint32_t group_1q = 4;
   uint32_t block_bits = 0;
   static FusionOptions none() { return FusionOptions{false, false, false, 1, 0}; }
+  static FusionOptions blocked(uint32_t bits) {
+    FusionOptions o;
+    o.block_bits = bits;
+    return o;
+  }
 };
 
 Plan build_plan(const Circuit &c, const FusionOptions &opts = {});

@@ -599,6 +599,17 @@ extern "C" unsigned int *qmk_wait_counter(void *ws) {
   return ws ? area_of(ws).waits : nullptr;
 }
 
+extern "C" int qmk_set_wait_poll_limit(void *ws, size_t bytes, long long polls, void *stream) {
+  if (!ok_ws(ws, bytes, 0)) return -1;
+  cudaStream_t s = (cudaStream_t)stream;
+  // Stored as polls + 1 (0 keeps the kernels' full bound), capped at it.
+  const unsigned int v =
+      polls < 0 ? 0u : static_cast<unsigned int>(std::min<long long>(polls, 1ll << 22) + 1);
+  cudaError_t e = cudaMemcpyAsync(area_of(ws).polls, &v, sizeof(v), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  return e == cudaSuccess ? 0 : static_cast<int>(e);
+}
+
 extern "C" int qmk_take_wait_timeouts(void *ws, size_t bytes, unsigned int *out, void *stream) {
   if (!out || !ok_ws(ws, bytes, 0)) return -1;
   cudaStream_t s = (cudaStream_t)stream;

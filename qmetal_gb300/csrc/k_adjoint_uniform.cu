@@ -77,7 +77,10 @@ __device__ __forceinline__ float split_one(float4 (&P)[kPairNV], float4 (&L)[kPa
 // bounded: a wait that gives up is counted in the workspace's wait counter
 // (Area::waits, read by the host after the pass), the warp stops streaming
 // and drains its copies in flight before it exits, and the kernel goes on,
-// so it cannot hang.
+// so it cannot hang. A test may shorten the bound of the in-loop waits
+// through the workspace (Area::polls; qmk_set_wait_poll_limit), down to
+// giving up at once; the drain before exit always keeps the full bound, so
+// every copy lands before its block ends.
 constexpr uint32_t kMaxWaitPolls = 1u << 22;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -117,10 +120,18 @@ __device__ __forceinline__ void fence_proxy_async() {
 }
 // Bounded wait for a phase of the barrier; false if it gave up. Called by a
 // whole warp, which reduces the answer to one warp-uniform flag.
-__device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity) {
-  for (uint32_t polls = 0; polls < kMaxWaitPolls; polls++)
+__device__ __forceinline__ bool mbar_wait(uint64_t *mb, uint32_t parity,
+                                          uint32_t limit = kMaxWaitPolls) {
+  for (uint32_t polls = 0; polls < limit; polls++)
     if (mbar_try_wait(mb, parity)) return true;
   return false;
+}
+
+// The in-loop wait bound of this workspace: the full bound unless a test set
+// one (stored as polls + 1, so that the zeroed workspace means the default).
+__device__ __forceinline__ uint32_t wait_limit(const Area &a) {
+  const uint32_t v = *a.polls;
+  return v == 0 ? kMaxWaitPolls : min(v - 1, kMaxWaitPolls);
 }
 
 // Four register wires on a warp pair (the fourth split across the pair),
@@ -179,7 +190,9 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   // to land.
   bool stalled = false;
   uint32_t stalled_parity = 0;
+  uint32_t limit = kMaxWaitPolls;
   if constexpr (kPipe) {
+    limit = wait_limit(a);
     if (lane == 0) mbar_init(&mbar[warp], 1);
     fence_proxy_async();
     __syncwarp();
@@ -209,7 +222,7 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     const uint64_t base = active ? base_of(ws) : 0;
     if constexpr (kPipe) {
       if (active && !stalled) {
-        const bool landed = mbar_wait(&mbar[warp], parity);
+        const bool landed = mbar_wait(&mbar[warp], parity, limit);
         if (!__all_sync(0xffffffffu, landed)) {
           if (lane == 0) atomicAdd(a.waits, 1u);
           stalled = true;
@@ -254,7 +267,10 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
     reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
     if constexpr (!kPipe) split_ops();
-    if (active) {
+    // A warp that gave up a wait computed on slots that may not have held
+    // this round's rows: it leaves the states alone (the host refuses the
+    // pass and resets the simulator's state).
+    if (active && !stalled) {
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         const uint64_t v = vec_of(base, l);

@@ -33,7 +33,9 @@ std::mutex g_lock;
 void *g_scratch_addr[kMaxDevices] = {nullptr};
 
 // The array's name is a host-side stand-in in host code; its device address
-// is looked up once per device, with that device current.
+// is looked up once per device, with that device current, and kept for the
+// process (a cudaDeviceReset would drop the array with the context, so the
+// entry point is documented as not usable on a device after a reset).
 int scratch_for_current_device(void **out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);

@@ -21,6 +21,7 @@ struct Area {
   double *partials;   // kMaxBlocks x 32
   unsigned *counter;  // last-block ticket, back to 0 after each reduction
   unsigned *waits;    // bounded waits that gave up in passes on this workspace
+  unsigned *polls;    // 0: waits take the full bound; k > 0: they give up after k - 1 polls
 };
 
 inline Area area_of(void *ws) {
@@ -29,6 +30,7 @@ inline Area area_of(void *ws) {
   a.partials = reinterpret_cast<double *>(b);
   a.counter = reinterpret_cast<unsigned *>(b + kMaxBlocks * 32 * sizeof(double));
   a.waits = a.counter + 16;  // 64 bytes into the 256-byte tail, its own line
+  a.polls = a.counter + 32;  // 128 bytes in: a test's poll limit for those waits
   return a;
 }
 

@@ -559,6 +559,13 @@ void Simulator::apply_op_to(float *st, const PlanOp &op) {
 // ---------------------------------------------------------------------------
 // State access
 
+std::vector<cdouble> Simulator::amplitudes() {
+  const float *f = raw();
+  std::vector<cdouble> out(dim());
+  for (size_t i = 0; i < out.size(); i++) out[i] = cdouble(f[2 * i], f[2 * i + 1]);
+  return out;
+}
+
 const float *Simulator::raw() {
   activate();
   const size_t bytes = dim() * 8;
@@ -600,9 +607,12 @@ void Simulator::fetch(size_t count, bool waits) {
                "wait count copy");
   synchronize();
   // Fail closed if a window-tile pass gave up a bounded wait (its results
-  // are not valid). The counter only grows; compare with the last look.
+  // are not valid, and neither are the states it left). The counter only
+  // grows; compare with the last look.
   if (waits && *h_waits_ != waits_seen_) {
     waits_seen_ = *h_waits_;
+    reset();
+    synchronize();
     throw std::runtime_error("adjoint window pass: a bulk-copy wait timed out");
   }
 }
@@ -612,7 +622,16 @@ void Simulator::check_waits() {
   unsigned int n = 0;
   check(qmk_take_wait_timeouts(ws_, ws_bytes_, &n, stream_), "wait check");
   waits_seen_ = 0;  // the take reset the counter
-  if (n) throw std::runtime_error("adjoint window pass: a bulk-copy wait timed out");
+  if (n) {
+    reset();
+    synchronize();
+    throw std::runtime_error("adjoint window pass: a bulk-copy wait timed out");
+  }
+}
+
+void Simulator::set_wait_poll_limit(long long polls) {
+  activate();
+  check(qmk_set_wait_poll_limit(ws_, ws_bytes_, polls, stream_), "wait poll limit");
 }
 
 // ---------------------------------------------------------------------------
@@ -724,6 +743,22 @@ void Simulator::launch_sample(size_t shots, uint64_t seed) {
         "sample");
   const uint64_t nb = ((uint64_t(1) << n_) + 1023) / 1024;
   dispatches_ += (nb > 2048) ? 5 : 3;
+}
+
+std::vector<std::pair<std::string, uint64_t>> Simulator::counts(size_t shots, uint64_t seed) {
+  std::map<uint64_t, uint64_t> tally;
+  for (uint64_t v : sample(shots, seed)) tally[v]++;
+  std::vector<std::pair<std::string, uint64_t>> out;
+  out.reserve(tally.size());
+  for (const auto &kv : tally) {
+    std::string bits(n_, '0');
+    for (uint32_t q = 0; q < n_; q++)
+      if ((kv.first >> q) & 1ull) bits[n_ - 1 - q] = '1';
+    out.emplace_back(std::move(bits), kv.second);
+  }
+  std::stable_sort(out.begin(), out.end(),
+                   [](const auto &a, const auto &b) { return a.second > b.second; });
+  return out;
 }
 
 std::vector<uint64_t> Simulator::sample(size_t shots, uint64_t seed) {
@@ -945,6 +980,10 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
     throw;
   }
   return {h_results_[0], grad};
+}
+
+std::vector<double> Simulator::gradient(const Circuit &c, const Hamiltonian &h) {
+  return energy_and_gradient(c, h).second;
 }
 
 // One serving request: forward once, draw the samples from the final state,

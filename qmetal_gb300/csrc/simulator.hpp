@@ -50,6 +50,8 @@ class Simulator {
   uint32_t num_qubits() const { return n_; }
   size_t dim() const { return size_t(1) << n_; }
 
+  // Amplitudes widened to complex128 (a host copy of the state).
+  std::vector<cdouble> amplitudes();
   const float *raw();                   // host mirror, refreshed
   void get_state(float *out);           // 2 * dim floats
   void set_state(const float *in);      // 2 * dim floats
@@ -61,6 +63,8 @@ class Simulator {
   void expectation_terms(const Hamiltonian &h, double *out);
 
   std::vector<uint64_t> sample(size_t shots, uint64_t seed = 0);
+  // Bitstring counts, most frequent first; qubit 0 is the rightmost character.
+  std::vector<std::pair<std::string, uint64_t>> counts(size_t shots, uint64_t seed = 0);
 
   // Adjoint energy and per-gate gradient. fused = true runs the block-wise
   // backward sweep (commuting blocks undone in one pass each); false runs the
@@ -68,6 +72,7 @@ class Simulator {
   std::pair<double, std::vector<double>> energy_and_gradient(const Circuit &c,
                                                              const Hamiltonian &h,
                                                              bool fused = true);
+  std::vector<double> gradient(const Circuit &c, const Hamiltonian &h);
 
   // Forward, samples from the final state, energy and block-wise gradient in
   // one queued sequence with a single synchronisation.
@@ -93,8 +98,13 @@ class Simulator {
   double elapsed();
 
   // Throws if a window pass on this simulator gave up a bounded wait since
-  // the last check (a copy and a synchronisation on its stream).
+  // the last check (a copy and a synchronisation on its stream). A pass
+  // that gave up leaves both states invalid, so the state is then reset to
+  // |0...0> before the throw, as a successful gradient's sweep also ends.
   void check_waits();
+  // Fault injection for tests: the window passes' bounded bulk-copy waits
+  // give up after `polls` polls (0: at once); negative restores the bound.
+  void set_wait_poll_limit(long long polls);
 
   static bool available();
   static std::string device_name();

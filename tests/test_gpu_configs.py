@@ -3,12 +3,16 @@
 1. QFT + swap layer at 22 qubits, gate by gate, from a seeded random
    normalised state: every amplitude against the complex128 oracle.
 2. The four fused 30-qubit workloads, checked against the oracle at 20 and 26
-   qubits (fused and gate by gate), and their norms at 30.
+   qubits (fused and gate by gate) and at 28 qubits (every amplitude against
+   the oracle's plan executor on all host threads), and their norms at 30.
 3. GHZ and QFT at 33 and 34 qubits without an oracle: norm, <Z_q>, GHZ
    <Z_0 Z_{n-1}> and 10^6 samples landing only on the two poles.
 4. Adjoint gradients of the HEA depth-8 problem through torch.autograd:
-   parameter shift on the oracle, central differences on the GPU.
+   parameter shift on the oracle, every entry against the oracle's adjoint
+   gradient at 22 qubits, the block-wise sweep against the gate-by-gate sweep
+   at 28 qubits, central differences on the GPU.
 """
+import os
 import math
 
 import numpy as np
@@ -65,6 +69,31 @@ def test_fused_workloads_vs_oracle(name, n):
         sim.run(c, fuse=fuse)
         err = np.abs(sim.get_state() - want).max()
         assert err <= 1e-5, (fuse, err)
+
+
+def max_abs_diff(a, b, chunk=1 << 24):
+    """max |a - b| over two long vectors, a chunk at a time (bounded memory)."""
+    worst = 0.0
+    for i in range(0, a.size, chunk):
+        worst = max(worst, float(np.abs(a[i:i + chunk] - b[i:i + chunk]).max()))
+    return worst
+
+
+@pytest.mark.parametrize("name", list(WORKLOADS))
+def test_fused_workloads_vs_oracle_plan_at_28(name):
+    """The 1e-5 amplitude bound at the largest width it is stated for: the
+    fused plan on the GPU against the complex128 oracle executing the same
+    plan op by op (Reference::run(const Plan&), src/reference.cpp:208-248;
+    the library's plans equal the reference's build_plan, tests/test_plan.py)."""
+    n = 28
+    gates = WORKLOADS[name](n)
+    c = W.to_circuit(n, gates)
+    oracle.set_threads(os.cpu_count() or 1)
+    want = oracle.run_plan(n, c.plan_export())
+    sim = qm.Simulator(n)
+    sim.run(c)
+    err = max_abs_diff(sim.get_state(), want)
+    assert err <= 1e-5, err
 
 
 @pytest.mark.parametrize("name", list(WORKLOADS))
@@ -163,7 +192,25 @@ def test_autograd_central_differences_and_chain_rule():
         assert abs(fd - phi.grad[k].item()) <= 2e-3 * max(1.0, abs(fd)), k
 
 
-def test_adjoint_gradient_at_28_qubits_is_consistent():
+def test_hea_d8_gradient_vs_oracle_adjoint_n22():
+    """Every one of the 352 gradient entries of the HEA depth-8 problem at 22
+    qubits against the complex128 oracle's adjoint gradient."""
+    n = 22
+    gates, terms = W.hea_gradient_problem(n, depth=8, seed=5)
+    sim = qm.Simulator(n)
+    e, g = sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+    oracle.set_threads(os.cpu_count() or 1)
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    assert sum(1 for x in gates if x[2]) == 2 * n * 8
+    assert abs(e - e0) <= 1e-4
+    assert float(np.max(np.abs(np.array(g) - g0))) <= 1e-5
+
+
+def test_adjoint_gradient_at_28_qubits_blockwise_vs_gate_by_gate():
+    """At 28 qubits (448 parameters) the block-wise sweep against the
+    reference's gate-by-gate sweep on the same GPU, entry by entry; both are
+    pinned to the oracle at smaller widths. Through torch.autograd, with a
+    central-difference sanity check on three entries."""
     torch = pytest.importorskip("torch")
     from qmetal_gb300.autograd import Template, energy
     n = 28
@@ -177,6 +224,11 @@ def test_adjoint_gradient_at_28_qubits_is_consistent():
     g = theta.grad.numpy()
     assert np.isfinite(e.item()) and np.all(np.isfinite(g))
     assert abs(e.item()) <= 2 * n
+    e1, g1 = sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms),
+                                     fused=False)
+    g1 = np.array(g1)[tpl.param_index]
+    assert abs(e.item() - e1) <= 1e-4
+    assert float(np.max(np.abs(g - g1))) <= 1e-5
     eps = 1e-3
     for j in (0, 100, 447):
         d = torch.zeros_like(theta)
