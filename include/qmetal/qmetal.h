@@ -202,6 +202,12 @@ int qm_energy_and_gradient_mode(qm_simulator s, qm_circuit c,
                                 const qm_hamiltonian *h, int mode,
                                 double *out_energy, double *out_grad);
 
+/* Tile shape of this simulator's block-wise backward sweep: the most wires
+ * >= 6 one window pass holds, 1..6 (up to four beside wire 0 and wires 1..5;
+ * five or six in passes over wires >= 6 that all carry one rotation
+ * sequence). Default 4; the batch autotuner picks it per width. */
+int qm_set_tile_high(qm_simulator s, uint32_t tile_high);
+
 /* Fault injection for tests of the fail-closed path: the bounded bulk-copy
  * waits inside this simulator's adjoint window passes give up after `polls`
  * polls (0: at once); a negative value restores the full bound. A gradient
@@ -241,9 +247,9 @@ int qm_batch_graph_timing(double *out_record_s, double *out_instantiate_s,
                           double *out_execute_s, uint64_t *out_nodes);
 
 /* Tune a batch on its own requests (their outputs are overwritten): per
- * width, the number of wires >= 6 each backward window pass holds in
- * registers (out_tile_high[n], qm_max_qubits() + 1 entries, may be NULL),
- * then the lane count. Cached per set of widths for the process. */
+ * width, the most wires >= 6 each backward window pass holds (1..6, as
+ * qm_set_tile_high; out_tile_high[n], qm_max_qubits() + 1 entries, may be
+ * NULL), then the lane count. Cached per set of widths for the process. */
 int qm_batch_autotune(const qm_batch_item *items, size_t count, uint32_t *out_lanes,
                       uint32_t *out_tile_high, double *out_seconds);
 

@@ -130,6 +130,7 @@ _energy_grad_mode = _decl("qm_energy_and_gradient_mode", c_int, c_void_p, c_void
                           POINTER(_Hamiltonian), c_int, _f64p, _f64p)
 _elapsed = _decl("qm_elapsed", c_int, c_void_p, _f64p)
 _wait_poll_limit = _decl("qm_set_wait_poll_limit", c_int, c_void_p, ctypes.c_int64)
+_set_tile_high = _decl("qm_set_tile_high", c_int, c_void_p, c_uint32)
 
 
 class _BatchItem(ctypes.Structure):
@@ -457,6 +458,12 @@ class Simulator:
         else:
             _check(_energy_grad_mode(self._h, circuit._h, byref(h), 1, byref(energy), grad))
         return energy.value, list(grad)[:len(circuit)]
+
+    def set_tile_high(self, tile_high: int):
+        """Wires >= 6 per backward window pass (1..6; five and six in block
+        tiles of uniform rotation layers)."""
+        _check(_set_tile_high(self._h, int(tile_high)))
+        return self
 
     def set_wait_poll_limit(self, polls: int):
         """Fault injection for tests: the adjoint window passes' bounded

@@ -13,6 +13,7 @@
 // The autotuner picks, from measurements on the batch's own requests, the
 // tile shape of the backward window passes per width and the lane count.
 #include "batch.hpp"
+#include "schedule.hpp"
 
 #include "../../include/qmetal/qmetal_kernels.h"
 
@@ -272,7 +273,7 @@ BatchTuning autotune_batch(const std::vector<BatchItem> &items) {
       }
     Simulator sim(n);
     double best_t = 1e300;
-    for (uint32_t kh = 1; kh <= std::min<uint32_t>(4, n - 6); kh++) {
+    for (uint32_t kh = 1; kh <= std::min<uint32_t>(kMaxTileHigh, n - 6); kh++) {
       sim.set_tile_high(kh);
       sim.serve(*req->circuit, *req->hamiltonian, req->shots, req->seed, req->energy, req->grad,
                 req->samples);

@@ -433,6 +433,18 @@ int qm_run_profiled(qm_simulator s, qm_circuit c, int fuse, double *out, size_t 
   });
 }
 
+int qm_set_tile_high(qm_simulator s, uint32_t tile_high) {
+  if (!s) {
+    set_error("null argument");
+    return -1;
+  }
+  if (tile_high < 1 || tile_high > kMaxTileHigh) {
+    set_error("tile_high must be 1..6");
+    return -1;
+  }
+  return guarded([&] { s->s->set_tile_high(tile_high); });
+}
+
 int qm_set_wait_poll_limit(qm_simulator s, int64_t polls) {
   if (!s) {
     set_error("null argument");

@@ -501,10 +501,12 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
   uint32_t distinct[kMaxWarpOps], high[kMaxWarpOps];
   uint32_t nd = 0, nh = 0;
   int ngrad = 0;
+  bool low = false;   // any wire below 6
   for (uint32_t o = 0; o < nops; o++) {
     if (wires[o] >= n || gens[o] < 0 || gens[o] > 3) return -1;
     if (gens[o] && (!slots || !d_grad)) return -1;
     if (gens[o]) ngrad++;
+    low |= wires[o] < 6;
     if (wires[o] == 0) continue;   // wire 0 pairs the lanes of every vector: no tile bit
     bool seen = false;
     for (uint32_t k = 0; k < nd; k++) seen |= distinct[k] == wires[o];
@@ -514,6 +516,36 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
     }
   }
   if (ngrad > 16) return -1;
+  if ((nh == 5 || nh == 6) && !low && n >= 6 + nh) {
+    // Block tile: only the compile-time (uniform) kernels take five or six
+    // wires >= 6 in one pass; any other tile of that shape is refused.
+    std::sort(high, high + nh);
+    WarpAdjArgs g{};
+    OutSlots<kMaxGen> out{};
+    out.p = d_grad;
+    g.nops = nops;
+    g.ngrad = static_cast<uint32_t>(ngrad);
+    for (uint32_t k = 0; k < nh; k++) g.hpos[k] = high[k] - 6;
+    int gi = 0;
+    for (uint32_t o = 0; o < nops; o++) {
+      g.kind[o] = 2;
+      g.arg[o] = static_cast<int8_t>(std::find(high, high + nh, wires[o]) - high);
+      g.gen[o] = static_cast<int8_t>(gens[o]);
+      g.m[o] = m2_from(minv + 8 * o);
+      g.cls[o] = m2_class(g.m[o]);
+      g.slotidx[o] = 0;
+      if (gens[o]) {
+        g.slotidx[o] = static_cast<int8_t>(gi);
+        out.slot[gi] = slots[o];
+        gi++;
+      }
+    }
+    const uint64_t nsites = 1ull << (n - 6 - nh);
+    const int rc = qmk_adj::launch_uniform(static_cast<int>(nh), reinterpret_cast<float4 *>(psi),
+                                           reinterpret_cast<float4 *>(lam), nsites, g, out,
+                                           area_of(ws), (cudaStream_t)stream);
+    return rc == 1 ? -1 : rc;
+  }
   if (nh <= 4 && n >= 6 + nh) {
     // Warp tile: lanes carry wires 1..5, registers the wires >= 6.
     std::sort(high, high + nh);

@@ -23,9 +23,9 @@ namespace {
 // Matrices of a uniform tile: op k of wire 0, of lane wire i, of register
 // wire j.
 struct UniArgs {
-  uint32_t hpos[4];   // wires >= 6: vector bit - 5, ascending
+  uint32_t hpos[6];   // wires >= 6: vector bit - 5, ascending
   uint32_t lbit[5];   // lane wires' vector bits, in op order
-  M2 m0[2], ml[5][2], mh[4][2];
+  M2 m0[2], ml[5][2], mh[6][2];
 };
 
 // The M ops of one wire: op k has class Ck and generator Gk.
@@ -342,6 +342,186 @@ k_adj_warp_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   finish<NOPS>(acc, NOPS, a, out);
 }
 
+// Five or six wires >= 6 per pass on a block tile: a site is 2^(3 + WB)
+// rows of 32 vectors of each state, held by 2^WB warps with eight vectors of
+// each state per thread. Register bits 0..2 of a thread are the site's first
+// three wires and its warp's index in the site the others, so the first three
+// wires' ops run in registers; the site then trades places through shared
+// memory -- WB of the register bits become warp bits and the warp bits
+// register bits -- and the remaining wires' ops run in registers too. One
+// shared-memory round trip per round replaces an exchange per op on a wire
+// split across warps. The rows stream in by bulk copies (one batch per warp:
+// the rows of its first layout), and the next round's copies go out once
+// every warp of the site has read its second layout, so they overlap the
+// second half of the arithmetic and the stores. Waits are bounded as in
+// k_adj_pair_uni. Stores go from the second layout: every warp store is
+// still one 512-byte row.
+template <int WB, int M, int C0, int G0, int C1, int G1>
+__global__ void __launch_bounds__(kThreads, 2)
+k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsites, UniArgs g,
+              Area a, OutSlots<M *(3 + WB)> out) {
+  constexpr int NV = 8;
+  constexpr int KH = 3 + WB;                  // wires >= 6 in the tile
+  constexpr int NW = 1 << WB;                 // warps per site
+  constexpr int SPB = (kThreads / 32) / NW;   // sites per block
+  constexpr int ROWS = NV * NW;               // rows of one state in a site
+  constexpr int NOPS = M * KH;
+  static_assert(SPB >= 1 && SPB * NW == kThreads / 32, "whole sites per block");
+  extern __shared__ __align__(16) float4 xb[];   // [site][state][row][32 lanes]
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t sib = warp / NW, wsl = warp % NW;
+  float4 *site_p = xb + static_cast<size_t>(sib) * 2 * ROWS * 32;
+  float4 *site_l = site_p + ROWS * 32;
+  const uint64_t per_round = static_cast<uint64_t>(gridDim.x) * SPB;
+  const uint64_t rounds = (nsites + per_round - 1) / per_round;
+  // Row of register vector l in the first layout (register bits = the
+  // site's wires 0..2, warp bits = wires 3..) and in the second (register
+  // bits = wires 3.., then the rest of wires 0..2; warp bits = wires 0..WB-1).
+  auto row_a = [&](int l) { return static_cast<uint32_t>(l) | (wsl << 3); };
+  auto row_b = [&](int l) {
+    const uint32_t lo = static_cast<uint32_t>(l) & ((1u << WB) - 1u);   // -> wires 3..
+    const uint32_t hi = static_cast<uint32_t>(l) >> WB;                 // -> wires WB..2
+    return wsl | (hi << WB) | (lo << 3);
+  };
+  auto site_of = [&](uint64_t r) {
+    return r * per_round + static_cast<uint64_t>(blockIdx.x) * SPB + sib;
+  };
+  auto row0_of = [&](uint64_t st) {
+    uint64_t b = st;
+#pragma unroll
+    for (int j = 0; j < KH; j++) b = ins0(b, g.hpos[j]);
+    return b << 5;
+  };
+  auto vec_of = [&](uint64_t row0, uint32_t row) {
+    uint64_t v = row0;
+#pragma unroll
+    for (int j = 0; j < KH; j++)
+      if ((row >> j) & 1u) v |= 1ull << (g.hpos[j] + 5);
+    return v;
+  };
+  auto site_sync = [&]() {
+    if constexpr (SPB == 1) {
+      __syncthreads();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(sib + 1), "r"(NW * 32) : "memory");
+    }
+  };
+  float accf[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
+  __shared__ uint64_t mbar[kThreads / 32];   // one per warp: its rows of the next round
+  uint32_t parity = 0;
+  bool stalled = false;
+  uint32_t stalled_parity = 0;
+  const uint32_t limit = wait_limit(a);
+  if (lane == 0) mbar_init(&mbar[warp], 1);
+  fence_proxy_async();
+  __syncthreads();
+  auto prefetch = [&](uint64_t r) {
+    const uint64_t st = site_of(r);
+    if (r < rounds && st < nsites && !stalled && lane == 0) {
+      const uint64_t row0 = row0_of(st);
+      fence_proxy_async();
+      mbar_expect_tx(&mbar[warp], 2 * NV * 32 * sizeof(float4));
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        const uint32_t row = row_a(l);
+        const uint64_t v = vec_of(row0, row);
+        bulk_row(site_p + row * 32, psi + v, 32 * sizeof(float4), &mbar[warp]);
+        bulk_row(site_l + row * 32, lam + v, 32 * sizeof(float4), &mbar[warp]);
+      }
+    }
+  };
+  prefetch(0);
+  for (uint64_t r = 0; r < rounds; r++) {
+    const uint64_t st = site_of(r);
+    const bool active = st < nsites;   // uniform over the site's warps
+    float4 P[NV], L[NV];
+    if (active) {
+      if (!stalled) {
+        const bool landed = mbar_wait(&mbar[warp], parity, limit);
+        if (!__all_sync(0xffffffffu, landed)) {
+          if (lane == 0) atomicAdd(a.waits, 1u);
+          stalled = true;
+          stalled_parity = parity;
+        }
+        parity ^= 1u;
+      }
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        P[l] = site_p[row_a(l) * 32 + lane];
+        L[l] = site_l[row_a(l) * 32 + lane];
+      }
+      reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf);
+      reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + M);
+      reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + 2 * M);
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        site_p[row_a(l) * 32 + lane] = P[l];
+        site_l[row_a(l) * 32 + lane] = L[l];
+      }
+    }
+    site_sync();   // the first layout is written back
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) {
+        P[l] = site_p[row_b(l) * 32 + lane];
+        L[l] = site_l[row_b(l) * 32 + lane];
+      }
+    }
+    site_sync();   // every warp has read its second layout: the slots are free
+    if (active) {
+      prefetch(r + 1);
+      reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[3], accf + 3 * M);
+      if constexpr (WB > 1) reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[4], accf + 4 * M);
+      if constexpr (WB > 2) reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[5], accf + 5 * M);
+      // A warp that gave up a wait leaves the states alone (the host refuses
+      // the pass and resets the simulator's state).
+      if (!stalled) {
+        const uint64_t row0 = row0_of(st);
+#pragma unroll
+        for (int l = 0; l < NV; l++) {
+          const uint64_t v = vec_of(row0, row_b(l)) | lane;
+          psi[v] = P[l];
+          lam[v] = L[l];
+        }
+      }
+    }
+  }
+  if (stalled && !__all_sync(0xffffffffu, mbar_wait(&mbar[warp], stalled_parity)) && lane == 0)
+    atomicAdd(a.waits, 1u);
+  double acc[NOPS];
+#pragma unroll
+  for (int t = 0; t < NOPS; t++) acc[t] = accf[t];
+  finish<NOPS>(acc, NOPS, a, out);
+}
+
+template <int WB, int M, int C0, int G0, int C1, int G1>
+int launch_blk(float4 *psi, float4 *lam, uint64_t nsites, const UniArgs &g, double *grad,
+               const uint32_t *slots, Area a, cudaStream_t s) {
+  constexpr int NOPS = M * (3 + WB);
+  constexpr int SPB = (kThreads / 32) >> WB;
+  OutSlots<NOPS> out{};
+  out.p = grad;
+  for (int t = 0; t < NOPS; t++) out.slot[t] = slots[t];
+  unsigned grid = grid_for(nsites, SPB);
+  grid = std::min<unsigned>(grid, reduce_grid());
+  const size_t smem = static_cast<size_t>(SPB) * 2 * (8 << WB) * 32 * sizeof(float4);
+  // The opt-in above 48 KiB is per device; set it once on each.
+  static std::atomic<bool> opted[64];   // zero-initialised: false
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (!opted[dev]) {
+    const cudaError_t e =
+        cudaFuncSetAttribute(k_adj_blk_uni<WB, M, C0, G0, C1, G1>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    opted[dev] = true;
+  }
+  k_adj_blk_uni<WB, M, C0, G0, C1, G1><<<grid, kThreads, smem, s>>>(psi, lam, nsites, g, a, out);
+  return launch_status();
+}
+
 template <bool W0, int NL, int M, int C0, int G0, int C1, int G1>
 int launch_pair(float4 *psi, float4 *lam, uint64_t nw, const UniArgs &g, double *grad,
                 const uint32_t *slots, Area a, cudaStream_t s) {
@@ -393,7 +573,7 @@ int kind_of(int cls, int gen) {
 
 int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjArgs &g,
                    const OutSlots<kMaxGen> &out, Area a, cudaStream_t s) {
-  if (kh < 1 || kh > 4 || g.nops < 1 || g.nops > 20) return 1;
+  if (kh < 1 || kh > 6 || g.nops < 1 || g.nops > 20) return 1;
   // Wires in op order (a wire's ops are consecutive), each with its ops.
   struct Wire {
     int kind, arg, n;
@@ -421,7 +601,7 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
     if (seq[k] < 0) return 1;
   }
   UniArgs u{};
-  for (int j = 0; j < 4; j++) u.hpos[j] = g.hpos[j];
+  for (int j = 0; j < 6; j++) u.hpos[j] = g.hpos[j];
   int w0 = 0, nl = 0, nh = 0;
   uint32_t slots[20];
   int order[16], no = 0;   // wires in kernel order: wire 0, lanes, registers by index
@@ -460,6 +640,24 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
   const bool wide = w0 == 1 && nl == 5, narrow = w0 == 0 && nl == 0;
   if (!wide && !narrow) return 1;
   double *p = out.p;
+  if (kh >= 5) {
+    if (!narrow) return 1;
+#define QMK_UNI_BLK(WB)                                                                        \
+  if (kh == 3 + WB) {                                                                          \
+    if (M == 1 && seq[0] == kRx) return launch_blk<WB, 1, kMatRx, 1, 0, 0>(psi, lam, nw, u, p, slots, a, s);   \
+    if (M == 1 && seq[0] == kRy) return launch_blk<WB, 1, kMatReal, 2, 0, 0>(psi, lam, nw, u, p, slots, a, s); \
+    if (M == 1) return launch_blk<WB, 1, kMatDiag, 3, 0, 0>(psi, lam, nw, u, p, slots, a, s);                  \
+    if (seq[0] == kRz && seq[1] == kRy)                                                        \
+      return launch_blk<WB, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);    \
+    if (seq[0] == kRy && seq[1] == kRz)                                                        \
+      return launch_blk<WB, 2, kMatReal, 2, kMatDiag, 3>(psi, lam, nw, u, p, slots, a, s);    \
+    return 1;                                                                                  \
+  }
+    QMK_UNI_BLK(2)
+    QMK_UNI_BLK(3)
+#undef QMK_UNI_BLK
+    return 1;
+  }
   if (M == 1 && kh == 4) {
     if (wide) {
       if (seq[0] == kRx) return launch_pair<true, 5, 1, kMatRx, 1, 0, 0>(psi, lam, nw, u, p, slots, a, s);

@@ -17,7 +17,8 @@ constexpr int kMaxWarpOps = 32;
 
 struct WarpAdjArgs {
   uint32_t nops, ngrad;
-  uint32_t hpos[4];              // wires >= 6: vector bit - 5, ascending
+  uint32_t hpos[6];              // wires >= 6: vector bit - 5, ascending (up to
+                                 // four in a warp tile, six in a block tile)
   int8_t kind[kMaxWarpOps];      // 0: wire 0, 1: lane bit, 2: register bit,
                                  // 3: the wire split across a warp pair
   int8_t arg[kMaxWarpOps];       // lane bit (0..4) or register index
@@ -45,6 +46,9 @@ __device__ __forceinline__ float overlap(int gen, float2 p0, float2 p1, float2 l
 // The backward pass of a window tile whose wires all carry the same short
 // rotation sequence (k_adjoint_uniform.cu). Returns 1 with nothing launched
 // when the tile is not of that form, else 0 or a CUDA error code.
+// kh is the tile's number of wires >= 6: 1..4 (warp and warp-pair tiles,
+// nwsites = 2^(n - 6 - kh) warp sites) or 5..6 (block tiles of four or eight
+// warps per site, wires >= 6 only; nwsites counts their sites the same way).
 int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nwsites, const WarpAdjArgs &g,
                    const qmk::OutSlots<kMaxGen> &slots, qmk::Area a, cudaStream_t s);
 

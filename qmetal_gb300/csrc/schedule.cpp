@@ -392,9 +392,46 @@ std::vector<Segment> segment_circuit(const Circuit &c) {
 // Every gradient of a commuting block is read at the block boundary and the
 // block is undone on both states in the same pass. Blocks before the first
 // parameterised one are never undone.
+namespace {
+
+// The structure the kernel layer finds in a 2x2 once narrowed to float (the
+// kMat* classes of kcommon.cuh): 3 diagonal, 1 real, 2 RX-like, 0 general.
+int narrowed_class(const cdouble m[4]) {
+  float f[8];
+  for (int k = 0; k < 4; k++) {
+    f[2 * k] = static_cast<float>(m[k].real());
+    f[2 * k + 1] = static_cast<float>(m[k].imag());
+  }
+  if (f[2] == 0.0f && f[3] == 0.0f && f[4] == 0.0f && f[5] == 0.0f) return 3;
+  if (f[1] == 0.0f && f[3] == 0.0f && f[5] == 0.0f && f[7] == 0.0f) return 1;
+  if (f[1] == 0.0f && f[7] == 0.0f && f[2] == 0.0f && f[4] == 0.0f) return 2;
+  return 0;
+}
+
+// A wire's ops (in undo order) as one of the rotation sequences the block
+// tiles compile in: one RX, RY or RZ, or RZ then RY, or RY then RZ. Returns
+// a nonzero code for each such sequence, 0 for any other.
+uint32_t uniform_signature(const std::vector<WireOp> &ops) {
+  if (ops.empty() || ops.size() > 2) return 0;
+  int kind[2];
+  for (size_t k = 0; k < ops.size(); k++) {
+    const int cls = narrowed_class(ops[k].minv), gen = ops[k].gen;
+    if (cls == 2 && gen == 1) kind[k] = 0;        // RX
+    else if (cls == 1 && gen == 2) kind[k] = 1;   // RY
+    else if (cls == 3 && gen == 3) kind[k] = 2;   // RZ
+    else return 0;
+  }
+  if (ops.size() == 1) return 1 + kind[0];
+  if ((kind[0] == 2 && kind[1] == 1) || (kind[0] == 1 && kind[1] == 2))
+    return 4 + kind[0];
+  return 0;
+}
+
+}  // namespace
+
 std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high) {
   const uint32_t n = c.num_qubits;
-  tile_high = std::min<uint32_t>(std::max<uint32_t>(tile_high, 1), 4);
+  tile_high = std::min<uint32_t>(std::max<uint32_t>(tile_high, 1), kMaxTileHigh);
   std::vector<BackwardStep> out;
   const auto segs = segment_circuit(c);
   size_t first = segs.size();
@@ -470,9 +507,14 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
     std::vector<WireOp> tile;
     uint32_t others = 0, highs = 0, grads = 0;
     bool tile_has_param = false;
+    bool tile_low = false;     // the tile holds a wire below 6
+    uint32_t tile_sig = 0;     // the rotation sequence all its wires share (0: none)
     const bool wide = n >= 6;
     const uint32_t max_ops = wide ? kWideWindowOps : kWindowOps;
-    const uint32_t max_high = wide ? std::min<uint32_t>(tile_high, n - 6) : 0;
+    // Up to four wires >= 6 per pass in a warp tile; five or six in a block
+    // tile, which holds only wires >= 6 that all carry one rotation sequence.
+    const uint32_t max_high = wide ? std::min<uint32_t>(std::min<uint32_t>(tile_high, 4), n - 6) : 0;
+    const uint32_t max_high_blk = wide ? std::min<uint32_t>(tile_high, n - 6) : 0;
     auto flush = [&]() {
       if (tile.empty()) return;
       if (undo || tile_has_param) {
@@ -484,6 +526,8 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
       tile.clear();
       others = highs = grads = 0;
       tile_has_param = false;
+      tile_low = false;
+      tile_sig = 0;
     };
     for (uint32_t w = 0; w < n; w++) {
       if (per_wire[w].empty()) continue;
@@ -513,16 +557,23 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
         continue;
       }
       bool full;
+      const uint32_t sig = w >= 6 ? uniform_signature(ops) : 0;
       if (wide) {
-        // Warp tiles: wire 0, wires 1..5 in the lanes, up to four wires >= 6.
-        full = tile.size() + ops.size() > max_ops || highs + need_high > max_high ||
+        // Warp tiles: wire 0, wires 1..5 in the lanes, up to four wires >= 6;
+        // block tiles: five or six wires >= 6 of one rotation sequence.
+        const bool blk = !tile_low && w >= 6 && sig != 0 && (tile.empty() || sig == tile_sig);
+        full = tile.size() + ops.size() > max_ops ||
+               highs + need_high > (blk ? max_high_blk : max_high) ||
                grads + wgrads > kWindowGrads;
+        if (!full && !blk && highs > max_high) full = true;   // a block tile takes no other wire
       } else {
         const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;
         full = tile.size() + ops.size() > kWindowOps || others + need_other > 3 ||
                grads + wgrads > cap;
       }
       if (full) flush();
+      tile_sig = tile.empty() ? sig : (sig == tile_sig ? sig : 0);
+      tile_low |= w < 6;
       tile.insert(tile.end(), ops.begin(), ops.end());
       others += need_other;
       highs += need_high;

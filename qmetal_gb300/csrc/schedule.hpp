@@ -123,8 +123,13 @@ struct BackwardStep {
 // Generators per diagonal-block pass (the kernel's largest slot count).
 constexpr uint32_t kDiagGensPerPass = 48;
 
+// Most wires >= 6 one window pass may hold: four in a warp tile, five or
+// six in a block tile (wires >= 6 only, one rotation sequence on every wire).
+constexpr uint32_t kMaxTileHigh = 6;
+
 // The sweep from the final state back to the first parameterised block.
-// tile_high: wires >= 6 one window pass holds in registers (1..4).
+// tile_high: wires >= 6 one window pass holds (1..6; above four only in block
+// tiles).
 std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high);
 
 // Inverse gate (src/metal/simulator.mm:786-799) and the generator code of a

@@ -89,9 +89,10 @@ class Simulator {
   void *stream() const { return stream_; }
 
   // Tile shape of the block-wise sweep's window passes: how many wires >= 6
-  // one two-state pass holds in registers (1..4, besides wire 0 and the five
-  // lane wires). Chosen per width by the batch autotuner.
-  void set_tile_high(uint32_t k) { tile_high_ = k < 1 ? 1 : (k > 4 ? 4 : k); }
+  // one two-state pass holds (1..6: up to four in warp tiles, besides wire 0
+  // and the five lane wires; five or six in block tiles of uniform rotation
+  // layers). Chosen per width by the batch autotuner.
+  void set_tile_high(uint32_t k) { tile_high_ = k < 1 ? 1 : (k > 6 ? 6 : k); }
   uint32_t tile_high() const { return tile_high_; }
 
   uint64_t dispatch_count() const { return dispatches_; }

@@ -142,7 +142,7 @@ def test_autotuned_lanes_and_tile_shapes():
     assert tuned["lanes"] in (2, 4, 8, 16)
     assert tuned["seconds"] > 0
     for n, k in tuned["tile_high"].items():
-        assert 1 <= k <= min(4, n - 6), (n, k)
+        assert 1 <= k <= min(6, n - 6), (n, k)
     again = qm.batch_autotune(items)
     assert again["lanes"] == tuned["lanes"] and again["tile_high"] == tuned["tile_high"]
     out = qm.batch_serve(items, mode=qm.BATCH_LANES, lanes=0)

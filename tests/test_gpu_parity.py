@@ -594,3 +594,34 @@ def test_gradients_on_the_smallest_states(n):
             e1, g1 = oracle.energy_and_gradient(m, gm, [(1.0, 0, 0, 1), (0.5, 1, 0, 0)])
             assert abs(e - e1) <= 1e-5 and np.abs(np.array(g) - g1).max() <= 1e-5, (mode, m)
             assert len(s) == 32 and all(0 <= x < (1 << m) for x in s)
+
+
+@pytest.mark.parametrize("tile_high", [5, 6])
+@pytest.mark.parametrize("n", [11, 12, 13, 14, 15, 16])
+def test_block_tiles_every_width(n, tile_high):
+    """Five- and six-wire block tiles (wires >= 6 only, four or eight warps
+    per site, one shared-memory transpose per round): an RX layer, an RY
+    layer, an RZ layer, an RY.RZ layer (RZ then RY backward) and an RZ.RY
+    layer on every wire, between CX ladders, against the oracle's adjoint;
+    the block-wise sweep with tile_high 4 (no block tiles) gives the same
+    gradient."""
+    rng = np.random.default_rng(1600 + 10 * n + tile_high)
+    ang = lambda: float(rng.uniform(-3, 3))
+    entangle = [(CX, (q, q + 1), ()) for q in range(n - 1)]
+    gates = [(H, (q,), ()) for q in range(n)] + entangle
+    for kind in (RX, RY, RZ):
+        gates += [(kind, (q,), (ang(),)) for q in range(n)] + entangle
+    for q in range(n):
+        gates += [(RY, (q,), (ang(),)), (RZ, (q,), (ang(),))]
+    gates += entangle
+    for q in range(n):
+        gates += [(RZ, (q,), (ang(),)), (RY, (q,), (ang(),))]
+    terms = W.ring_tfim_hamiltonian(n, 0.7) + [(0.3, 0, 1 << 2, 1 << (n - 1))]
+    c, h = W.to_circuit(n, gates), W.to_hamiltonian(terms)
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    sim = qm.Simulator(n).set_tile_high(tile_high)
+    e1, g1 = sim.energy_and_gradient(c, h)
+    assert abs(e1 - e0) <= 1e-5
+    assert np.abs(np.array(g1) - g0).max() <= 1e-5
+    e2, g2 = qm.Simulator(n).set_tile_high(4).energy_and_gradient(c, h)
+    assert np.abs(np.array(g1) - np.array(g2)).max() <= 1e-5

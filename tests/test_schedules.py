@@ -242,6 +242,22 @@ def replay_costate(n, psi, terms):
     return lam, covered
 
 
+def rotation_kind(minv, gen):
+    """The rotation an undo matrix and generator describe, as the block tiles
+    see it (after narrowing to float): rx, ry, rz, or None."""
+    m = np.asarray(minv).reshape(2, 2).astype(np.complex64)
+    diag = m[0, 1] == 0 and m[1, 0] == 0
+    real = np.all(m.imag == 0)
+    rxl = m[0, 0].imag == 0 and m[1, 1].imag == 0 and m[0, 1].real == 0 and m[1, 0].real == 0
+    if diag and gen == 3:
+        return "rz"
+    if not diag and real and gen == 2:
+        return "ry"
+    if not diag and not real and rxl and gen == 1:
+        return "rx"
+    return None
+
+
 def replay_backward(n, gates, terms, tile_high):
     c = W.to_circuit(n, gates)
     steps = decode_backward(c.schedule_export("backward", tile_high=tile_high))
@@ -255,7 +271,16 @@ def replay_backward(n, gates, terms, tile_high):
             wires = {w for w, _, _, _ in ops}
             if n >= 6:
                 assert len(ops) <= 32
-                assert len({w for w in wires if w >= 6}) <= min(tile_high, n - 6)
+                high = len({w for w in wires if w >= 6})
+                assert high <= min(tile_high, n - 6)
+                if high > 4:
+                    # a block tile: wires >= 6 only, one rotation sequence each
+                    assert min(wires) >= 6 and high <= 6
+                    seqs = {tuple(rotation_kind(m, g) for ww, m, g, _ in ops if ww == w)
+                            for w in wires}
+                    assert len(seqs) == 1, seqs
+                    seq = seqs.pop()
+                    assert seq in {("rx",), ("ry",), ("rz",), ("rz", "ry"), ("ry", "rz")}, seq
             else:
                 assert len(ops) <= 16
             assert sum(g != 0 for _, _, g, _ in ops) <= 16
@@ -356,6 +381,13 @@ def gradient_problems():
                     W.maxcut_hamiltonian(edges)))
     out.append(("tfim9", 9, W.tfim_chain(9, steps=4), W.ring_tfim_hamiltonian(9)))
     out.append(("u3_10", 10, W.random_u3(10, depth=3), one_flip_terms(10, 2)))
+    # Wide enough for block tiles (five or six wires >= 6 of one rotation
+    # sequence after the first tile of a layer).
+    for n in (13, 14):
+        out.append((f"hea{n}", n) + W.hea_gradient_problem(n, depth=2))
+    edges = W.random_3regular(16, rng)
+    out.append(("maxcut16", 16, W.maxcut_qaoa(16, edges, [0.4, 1.1], [0.7, 0.2]),
+                W.maxcut_hamiltonian(edges)))
     return out
 
 
@@ -402,7 +434,19 @@ def test_costate_schedule_edge_cases():
     assert all(s[0] != "local" for s in steps)
 
 
-@pytest.mark.parametrize("tile_high", [1, 2, 4])
+@pytest.mark.parametrize("name,widest", [("hea13", 5), ("hea14", 6), ("maxcut16", 6)])
+def test_block_tiles_form_for_uniform_layers(name, widest):
+    """Rotation layers past the first tile go five or six wires >= 6 per pass
+    with tile_high 6, and never more than four with tile_high 4."""
+    _, n, gates, _ = next(p for p in PROBLEMS if p[0] == name)
+    c = W.to_circuit(n, gates)
+    for th, want in ((6, widest), (4, 4)):
+        steps = decode_backward(c.schedule_export("backward", tile_high=th))
+        high = [len({w for w, _, _, _ in s[1] if w >= 6}) for s in steps if s[0] == "window"]
+        assert max(high) == want, (th, high)
+
+
+@pytest.mark.parametrize("tile_high", [1, 2, 4, 5, 6])
 @pytest.mark.parametrize("name,n,gates,terms", PROBLEMS, ids=[p[0] for p in PROBLEMS])
 def test_backward_schedule_gradient(name, n, gates, terms, tile_high):
     grad, touched, steps = replay_backward(n, gates, terms, tile_high)
@@ -497,7 +541,7 @@ def test_random_circuits_replay_property():
         terms = random_terms(n, 5, seed) + one_flip_terms(n, seed)[:4]
         state, _ = replay_forward(n, gates)
         assert np.abs(state - oracle.run(n, gates)).max() < 1e-12
-        tile_high = data.draw(st.integers(1, 4))
+        tile_high = data.draw(st.integers(1, 6))
         grad, touched, _ = replay_backward(n, gates, terms, tile_high)
         _, want = oracle.energy_and_gradient(n, gates, terms)
         assert np.abs(grad - want).max() < 1e-10
