@@ -205,7 +205,8 @@ int qm_energy_and_gradient_mode(qm_simulator s, qm_circuit c,
 /* Tile shape of this simulator's block-wise backward sweep: the most wires
  * >= 6 one window pass holds, 1..6 (up to four beside wire 0 and wires 1..5;
  * five or six in passes over wires >= 6 that all carry one rotation
- * sequence). Default 4; the batch autotuner picks it per width. */
+ * sequence, a run of such wires split evenly over its passes). Default 6;
+ * the batch autotuner picks it per width. */
 int qm_set_tile_high(qm_simulator s, uint32_t tile_high);
 
 /* Fault injection for tests of the fail-closed path: the bounded bulk-copy

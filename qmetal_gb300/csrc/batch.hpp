@@ -44,7 +44,7 @@ struct BatchTuning {
   uint32_t tile_high[kMaxQubits + 1];
   double seconds = 0.0;   // time spent measuring
   BatchTuning() {
-    for (auto &t : tile_high) t = 4;
+    for (auto &t : tile_high) t = 6;   // the simulator default
   }
 };
 

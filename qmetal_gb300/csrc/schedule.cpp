@@ -529,10 +529,10 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
       tile_low = false;
       tile_sig = 0;
     };
+    // Each wire's ops in undo order, and the rotation sequence they form.
+    std::vector<std::vector<WireOp>> wire_ops(n);
+    std::vector<uint32_t> wire_sig(n, 0);
     for (uint32_t w = 0; w < n; w++) {
-      if (per_wire[w].empty()) continue;
-      std::vector<WireOp> ops;
-      uint32_t wgrads = 0;
       for (size_t r = per_wire[w].size(); r-- > 0;) {
         const size_t k = per_wire[w][r];
         const Gate &g = c.ops[k];
@@ -542,9 +542,31 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
         gate_matrix_1q(inv.kind, inv.params, o.minv);
         o.gen = g.num_params > 0 ? generator_of(g) : 0;
         o.slot = static_cast<uint32_t>(k);
-        if (o.gen) wgrads++;
-        ops.push_back(o);
+        wire_ops[w].push_back(o);
       }
+      if (w >= 6) wire_sig[w] = uniform_signature(wire_ops[w]);
+    }
+    // The block tiles of a run of wires sharing one rotation sequence split
+    // it evenly: a run of R wires takes ceil(R / tile_high) passes of at most
+    // ceil(R / passes) wires each (twenty wires: five passes of four become
+    // four of five, not three of six and one of two).
+    uint32_t blk_cap = max_high_blk;
+    auto balanced_cap = [&](uint32_t w) {
+      uint32_t run = 0;
+      for (uint32_t v = w; v < n; v++) {
+        if (wire_ops[v].empty()) continue;
+        if (wire_sig[v] != wire_sig[w]) break;
+        run++;
+      }
+      if (run == 0 || max_high_blk == 0) return max_high_blk;
+      const uint32_t passes = (run + max_high_blk - 1) / max_high_blk;
+      return (run + passes - 1) / passes;
+    };
+    for (uint32_t w = 0; w < n; w++) {
+      if (per_wire[w].empty()) continue;
+      const std::vector<WireOp> &ops = wire_ops[w];
+      uint32_t wgrads = 0;
+      for (const WireOp &o : ops) wgrads += o.gen != 0;
       const uint32_t need_other = w != 0 ? 1u : 0u, need_high = w >= 6 ? 1u : 0u;
       if (ops.size() > max_ops || wgrads > kWindowGrads) {
         flush();
@@ -557,13 +579,14 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
         continue;
       }
       bool full;
-      const uint32_t sig = w >= 6 ? uniform_signature(ops) : 0;
+      const uint32_t sig = wire_sig[w];
       if (wide) {
         // Warp tiles: wire 0, wires 1..5 in the lanes, up to four wires >= 6;
         // block tiles: five or six wires >= 6 of one rotation sequence.
         const bool blk = !tile_low && w >= 6 && sig != 0 && (tile.empty() || sig == tile_sig);
+        if (blk && tile.empty()) blk_cap = balanced_cap(w);
         full = tile.size() + ops.size() > max_ops ||
-               highs + need_high > (blk ? max_high_blk : max_high) ||
+               highs + need_high > (blk ? std::max(blk_cap, max_high) : max_high) ||
                grads + wgrads > kWindowGrads;
         if (!full && !blk && highs > max_high) full = true;   // a block tile takes no other wire
       } else {
@@ -572,6 +595,7 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
                grads + wgrads > cap;
       }
       if (full) flush();
+      if (tile.empty() && w >= 6 && sig != 0) blk_cap = balanced_cap(w);   // a new tile opens
       tile_sig = tile.empty() ? sig : (sig == tile_sig ? sig : 0);
       tile_low |= w < 6;
       tile.insert(tile.end(), ops.begin(), ops.end());

@@ -91,7 +91,7 @@ class Simulator {
   // Tile shape of the block-wise sweep's window passes: how many wires >= 6
   // one two-state pass holds (1..6: up to four in warp tiles, besides wire 0
   // and the five lane wires; five or six in block tiles of uniform rotation
-  // layers). Chosen per width by the batch autotuner.
+  // layers; default 6). Chosen per width by the batch autotuner.
   void set_tile_high(uint32_t k) { tile_high_ = k < 1 ? 1 : (k > 6 ? 6 : k); }
   uint32_t tile_high() const { return tile_high_; }
 
@@ -160,7 +160,7 @@ class Simulator {
   bool mirror_pinned_ = false;
   void *ev_start_ = nullptr, *ev_stop_ = nullptr;
   uint64_t dispatches_ = 0;
-  uint32_t tile_high_ = 4;
+  uint32_t tile_high_ = 6;
   struct GraphEntry {
     uint64_t key;
     void *exec;         // cudaGraphExec_t
