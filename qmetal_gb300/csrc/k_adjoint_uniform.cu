@@ -406,6 +406,14 @@ k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsite
       asm volatile("bar.sync %0, %1;" ::"r"(sib + 1), "r"(NW * 32) : "memory");
     }
   };
+  // Each warp's eight row offsets (the row's wire bits, as a vector index)
+  // in both layouts, worked out once: a round then adds them to its site's
+  // first row instead of testing six wire bits per vector.
+  __shared__ uint64_t row_off[kThreads / 32][2][NV];
+  if (lane < 2 * NV) {
+    const int l = lane & (NV - 1);
+    row_off[warp][lane / NV][l] = vec_of(0, lane < NV ? row_a(l) : row_b(l));
+  }
   float accf[NOPS];
 #pragma unroll
   for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
@@ -426,7 +434,7 @@ k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsite
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         const uint32_t row = row_a(l);
-        const uint64_t v = vec_of(row0, row);
+        const uint64_t v = row0 | row_off[warp][0][l];
         bulk_row(site_p + row * 32, psi + v, 32 * sizeof(float4), &mbar[warp]);
         bulk_row(site_l + row * 32, lam + v, 32 * sizeof(float4), &mbar[warp]);
       }
@@ -478,10 +486,10 @@ k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsite
       // A warp that gave up a wait leaves the states alone (the host refuses
       // the pass and resets the simulator's state).
       if (!stalled) {
-        const uint64_t row0 = row0_of(st);
+        const uint64_t row0 = row0_of(st) | lane;
 #pragma unroll
         for (int l = 0; l < NV; l++) {
-          const uint64_t v = vec_of(row0, row_b(l)) | lane;
+          const uint64_t v = row0 | row_off[warp][1][l];
           psi[v] = P[l];
           lam[v] = L[l];
         }
