@@ -259,6 +259,101 @@ k_group5_pair(float4 *__restrict__ st, uint64_t nsites, GroupArgs g) {
   }
 }
 
+// Six or seven wires >= 6 in one pass (optionally with wire 0) on a block
+// of warps: a site is 2^(4 + WB) rows of 32 vectors, held by 2^WB warps with
+// sixteen vectors per thread. A thread's four register bits are the site's
+// first four wires and its warp's index the others, so those four wires'
+// 2x2s run in registers; the site then trades places through shared memory
+// (WB register bits become warp bits and the warp bits register bits) and
+// the last WB wires run in registers too. One shared-memory round trip per
+// site instead of a pair exchange per wire; every load and store is a
+// 512-byte warp row.
+struct BlkGroupArgs {
+  uint32_t pos[7];   // the wires' vector bits (wire - 1), ascending, all >= 5
+  M2 m[7];
+  M2 m0;             // wire 0 when W0
+};
+
+template <int WB, bool W0, int CLS>
+__global__ void __launch_bounds__(kThreads, 2)
+k_group_blk(float4 *__restrict__ st, uint64_t nsites, BlkGroupArgs g) {
+  constexpr int NV = 16;
+  constexpr int KB = 4 + WB;                  // wires >= 6 in the group
+  constexpr int NW = 1 << WB;                 // warps per site
+  constexpr int SPB = (kThreads / 32) / NW;   // sites per block
+  constexpr int ROWS = NV * NW;
+  static_assert(SPB >= 1 && SPB * NW == kThreads / 32, "whole sites per block");
+  extern __shared__ __align__(16) float4 xq[];   // [site][row][32 lanes]
+  const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const uint32_t sib = warp / NW, wsl = warp % NW;
+  float4 *site = xq + static_cast<size_t>(sib) * ROWS * 32;
+  const uint64_t sidx = static_cast<uint64_t>(blockIdx.x) * SPB + sib;
+  const bool active = sidx < nsites;   // uniform over the site's warps
+  // Rows in the first layout (register bits = wires 0..3 of the group, warp
+  // bits = wires 4..) and the second (register bits = wires 4.., then wires
+  // WB..3; warp bits = wires 0..WB-1); each warp's offsets worked out once.
+  auto row_a = [&](int l) { return static_cast<uint32_t>(l) | (wsl << 4); };
+  auto row_b = [&](int l) {
+    const uint32_t lo = static_cast<uint32_t>(l) & (NW - 1u), hi = static_cast<uint32_t>(l) >> WB;
+    return wsl | (hi << WB) | (lo << 4);
+  };
+  __shared__ uint64_t row_off[kThreads / 32][2][NV];
+  {
+    const int l = lane & (NV - 1);
+    const uint32_t row = lane < NV ? row_a(l) : row_b(l);
+    uint64_t v = 0;
+#pragma unroll
+    for (int j = 0; j < KB; j++)
+      if ((row >> j) & 1u) v |= 1ull << g.pos[j];
+    row_off[warp][lane / NV][l] = v;
+  }
+  __syncwarp();
+  uint64_t base = sidx * 32 + lane;
+#pragma unroll
+  for (int j = 0; j < KB; j++) base = ins0(base, g.pos[j]);
+  float4 r[NV];
+#pragma unroll
+  for (int l = 0; l < NV; l++)
+    r[l] = active ? st[base | row_off[warp][0][l]] : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (W0) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      float2 x = lo2(r[l]), y = hi2(r[l]);
+      apply2c(CLS, g.m0, x, y);
+      r[l] = pack4(x, y);
+    }
+  }
+  auto reg_wire = [&](int j, const M2 &m) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) {
+      if ((l >> j) & 1) continue;
+      const int h = l | (1 << j);
+      float2 a0 = lo2(r[l]), b0 = lo2(r[h]), a1 = hi2(r[l]), b1 = hi2(r[h]);
+      apply2c(CLS, m, a0, b0);
+      apply2c(CLS, m, a1, b1);
+      r[l] = pack4(a0, a1);
+      r[h] = pack4(b0, b1);
+    }
+  };
+#pragma unroll
+  for (int j = 0; j < 4; j++) reg_wire(j, g.m[j]);
+#pragma unroll
+  for (int l = 0; l < NV; l++) site[row_a(l) * 32 + lane] = r[l];
+  if constexpr (SPB == 1) {
+    __syncthreads();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(sib + 1), "r"(NW * 32) : "memory");
+  }
+#pragma unroll
+  for (int l = 0; l < NV; l++) r[l] = site[row_b(l) * 32 + lane];
+#pragma unroll
+  for (int j = 0; j < WB; j++) reg_wire(j, g.m[4 + j]);
+  if (active) {
+#pragma unroll
+    for (int l = 0; l < NV; l++) st[base | row_off[warp][1][l]] = r[l];
+  }
+}
+
 struct WarpGroupArgs {
   uint32_t nlow;     // wires 1..5: lane bits
   uint32_t lbit[5];  // their vector bits (0..4)
@@ -655,6 +750,36 @@ static int launch_group5_pair_cls(float4 *st, uint64_t nsites, const GroupArgs &
   return launch_status();
 }
 
+template <int WB, bool W0, int CLS>
+static int launch_group_blk_cls(float4 *st, uint64_t nsites, const BlkGroupArgs &g,
+                                cudaStream_t s) {
+  constexpr int SPB = (kThreads / 32) >> WB;
+  const size_t smem = static_cast<size_t>(SPB) * (16 << WB) * 32 * sizeof(float4);
+  // The opt-in above 48 KiB is per device; set it once on each.
+  static std::atomic<bool> opted[64];   // zero-initialised: false
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return -1;
+  if (!opted[dev]) {
+    const cudaError_t e = cudaFuncSetAttribute(
+        k_group_blk<WB, W0, CLS>, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem));
+    if (e != cudaSuccess) return static_cast<int>(e);
+    opted[dev] = true;
+  }
+  k_group_blk<WB, W0, CLS><<<grid_for(nsites, SPB), kThreads, smem, s>>>(st, nsites, g);
+  return launch_status();
+}
+
+template <int WB, bool W0>
+static int launch_group_blk(float4 *st, uint64_t nsites, const BlkGroupArgs &g, int cls,
+                            cudaStream_t s) {
+  switch (cls) {
+    case kMatDiag: return launch_group_blk_cls<WB, W0, kMatDiag>(st, nsites, g, s);
+    case kMatRx: return launch_group_blk_cls<WB, W0, kMatRx>(st, nsites, g, s);
+    case kMatReal: return launch_group_blk_cls<WB, W0, kMatReal>(st, nsites, g, s);
+    default: return launch_group_blk_cls<WB, W0, kMatGeneral>(st, nsites, g, s);
+  }
+}
+
 template <bool W0>
 static int launch_group5_pair(float4 *st, uint64_t nsites, const GroupArgs &g, int cls,
                               cudaStream_t s) {
@@ -729,6 +854,34 @@ extern "C" int qmk_apply_group(float *state, uint32_t n, uint32_t k,
         default: return -1;
       }
       return launch_status();
+    }
+  }
+  {
+    // Six or seven wires >= 6 (and perhaps wire 0): the block route.
+    const uint32_t kh = k - (w0 ? 1u : 0u);
+    bool high_only = true;
+    for (uint32_t j = 0; j < k; j++) high_only &= qubits[j] == 0 || qubits[j] >= 6;
+    if (high_only && (kh == 6 || kh == 7) && n - 1 >= 5 + kh) {
+      BlkGroupArgs bg{};
+      uint32_t kb = 0;
+      std::vector<M2> all;
+      for (uint32_t j = 0; j < k; j++) {
+        const M2 m = m2_from(mats + 8 * j);
+        all.push_back(m);
+        if (qubits[j] == 0) {
+          bg.m0 = m;
+        } else {
+          bg.pos[kb] = qubits[j] - 1;
+          bg.m[kb] = m;
+          kb++;
+        }
+      }
+      const int cls = common_class(all.data(), static_cast<int>(k));
+      const uint64_t nsites = 1ull << (n - 1 - 5 - kh);
+      if (kh == 6) return w0 ? launch_group_blk<2, true>(st, nsites, bg, cls, s)
+                             : launch_group_blk<2, false>(st, nsites, bg, cls, s);
+      return w0 ? launch_group_blk<3, true>(st, nsites, bg, cls, s)
+                : launch_group_blk<3, false>(st, nsites, bg, cls, s);
     }
   }
   if (k - (w0 ? 1u : 0u) > 5) return -1;  // register path: at most five wires >= 1

@@ -116,6 +116,7 @@ std::vector<ForwardStep> merged_schedule(const Plan &p) {
     }
     if (zero > 1) return false;
     if (lane >= 1 && lane <= 5 && high <= 4 && n >= 6 + high) return true;
+    if (lane == 0 && high >= 6 && high <= 7 && n >= 6 + high) return true;   // block groups
     return lane + high <= 5;
   };
   auto flush = [&]() {

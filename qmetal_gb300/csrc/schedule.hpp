@@ -57,8 +57,9 @@ struct ForwardStep {
 
 // The plan with consecutive one-qubit ops merged into group passes (wire 0,
 // up to five of wires 1..5 and four wires >= 6; or wire 0 and five wires
-// >= 1) and runs of CX / SWAP ops turned into one gather pass where that
-// moves fewer bytes. Every other op passes through. Same unitary as the plan.
+// >= 1; or wire 0 and six or seven wires >= 6) and runs of CX / SWAP ops
+// turned into one gather pass where that moves fewer bytes. Every other op
+// passes through. Same unitary as the plan.
 std::vector<ForwardStep> merged_schedule(const Plan &p);
 
 // --- co-state lambda = H psi and the energy ---------------------------------

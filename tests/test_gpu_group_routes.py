@@ -2,7 +2,8 @@
 
 One launch applies k commuting 2x2s on distinct wires: wire 0 within a
 vector, wires 1..5 by warp shuffle, up to four wires >= 6 in registers
-(k <= 10), or wire 0 plus up to five others in registers. Each case draws a
+(k <= 10), wire 0 plus up to five others in registers, or wire 0 plus six or
+seven wires >= 6 on a block of warps (one shared-memory transpose). Each case draws a
 wire set for one route and compares the state with the same matrices applied
 one wire at a time in complex128 (tolerance 1e-5, as the other amplitude
 tests). Wire sets outside every route must be rejected without a launch.
@@ -62,6 +63,12 @@ def _route_cases(n, rng):
     if n >= 11:
         cases.append(sorted(rng.choice(np.arange(6, n), size=5, replace=False).tolist()))
         cases.append([1, 3] + sorted(rng.choice(np.arange(6, n), size=3, replace=False).tolist()))
+    # block route: six or seven wires >= 6, with and without wire 0
+    for k in (6, 7):
+        if n >= 6 + k:
+            for w0 in (False, True):
+                high = sorted(rng.choice(np.arange(6, n), size=k, replace=False).tolist())
+                cases.append(([0] if w0 else []) + high)
     return cases
 
 
@@ -76,7 +83,7 @@ def _structured(rng, kind):
     return np.diag([np.exp(-0.5j * t), np.exp(0.5j * t)])
 
 
-@pytest.mark.parametrize("n", [6, 7, 9, 10, 11, 14])
+@pytest.mark.parametrize("n", [6, 7, 9, 10, 11, 12, 14])
 def test_every_route_matches_complex128(n):
     torch = pytest.importorskip("torch")
     L = _lib()
@@ -115,7 +122,7 @@ def test_rejects_wire_sets_outside_every_route():
     flat = np.tile(np.array([1, 0, 0, 0, 0, 0, 1, 0], dtype=np.float32), 11)
     bad = [
         [1, 6, 7, 8, 9, 10],          # five wires >= 6 beside a lane wire
-        [0, 6, 7, 8, 9, 10, 11],      # six register wires beside wire 0
+        [0, 1, 6, 7, 8, 9, 10, 11],   # six wires >= 6 beside a lane wire
         [3, 2],                       # not ascending
         [4, 4],                       # repeated
         [0, 12],                      # out of range

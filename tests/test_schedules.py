@@ -187,7 +187,8 @@ def replay_forward(n, gates):
             lane = sum(1 <= w <= 5 for w in wires)
             high = sum(w >= 6 for w in wires)
             assert zero <= 1
-            assert (1 <= lane <= 5 and high <= 4 and n >= 6 + high) or lane + high <= 5
+            assert ((1 <= lane <= 5 and high <= 4 and n >= 6 + high) or lane + high <= 5
+                    or (lane == 0 and high <= 7 and n >= 6 + high))
             for w, m in s[1]:
                 st = apply_1q(st, n, w, m)
         elif s[0] == "permute":
