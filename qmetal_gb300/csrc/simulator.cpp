@@ -156,6 +156,10 @@ void Simulator::release() {
   cudaFree(costate_);
   cudaFree(scratch_);
   scratch_ = nullptr;
+  for (const Checkpoint &c : ckpts_) cudaFree(c.buf);
+  ckpts_.clear();
+  for (float *b : ck_free_) cudaFree(b);
+  ck_free_.clear();
   cudaFree(ws_);
   cudaFree(sample_ws_);
   cudaFree(d_shots_);
@@ -216,6 +220,54 @@ bool Simulator::ensure_scratch() {
 void Simulator::invalidate_graphs() {
   for (const GraphEntry &e : graphs_) cudaGraphExecDestroy(static_cast<cudaGraphExec_t>(e.exec));
   graphs_.clear();
+}
+
+float *Simulator::take_buffer() {
+  if (!ck_free_.empty()) {
+    float *b = ck_free_.back();
+    ck_free_.pop_back();
+    return b;
+  }
+  constexpr size_t kMaxBuffers = 16;
+  if (ckpts_.size() >= kMaxBuffers) return nullptr;
+  const size_t bytes = dim() * 8;
+  size_t free_b = 0, total_b = 0;
+  float *b = nullptr;
+  // Keep 4 GiB of headroom for other simulators and the runtime.
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || free_b < bytes + (4ull << 30) ||
+      cudaMalloc(&b, bytes) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return b;
+}
+
+void Simulator::drop_checkpoints() {
+  for (const Checkpoint &c : ckpts_) ck_free_.push_back(c.buf);
+  ckpts_.clear();
+}
+
+// The top checkpoint, if the undo gather (cols, off) inverts the forward
+// gather it was taken at: dst1[y] = src[A y ^ a], dst2[z] = dst1[B z ^ b]
+// is the identity when A B = I and A b ^ a = 0.
+bool Simulator::restore_checkpoint(const std::vector<uint64_t> &cols, uint64_t off) {
+  if (ckpts_.empty()) return false;
+  const Checkpoint &c = ckpts_.back();
+  if (c.cols.size() != n_ || cols.size() != n_) return false;
+  auto apply = [&](uint64_t x) {
+    uint64_t y = 0;
+    for (uint32_t k = 0; k < n_; k++)
+      if ((x >> k) & 1ull) y ^= c.cols[k];
+    return y;
+  };
+  for (uint32_t j = 0; j < n_; j++)
+    if (apply(cols[j]) != (1ull << j)) return false;
+  if ((apply(off) ^ c.off) != 0) return false;
+  ck_free_.push_back(state_);
+  state_ = c.buf;
+  ckpts_.pop_back();
+  invalidate_graphs();   // captured graphs hold the old state pointer
+  return true;
 }
 
 bool Simulator::permute(float *&buf, const std::vector<uint64_t> &cols, uint64_t off) {
@@ -400,10 +452,22 @@ void Simulator::run_merged(const Plan &p) {
         dispatches_++;
         break;
       }
-      case ForwardStep::Permute:
+      case ForwardStep::Permute: {
+        if (keep_ckpts_ && ensure_scratch()) {
+          if (float *dst = take_buffer()) {
+            check(qmk_apply_permutation(dst, state_, n_, st.cols.data(), st.off, stream_),
+                  "permutation");
+            dispatches_++;
+            ckpts_.push_back({state_, st.cols, st.off});
+            state_ = dst;
+            invalidate_graphs();
+            break;
+          }
+        }
         if (!permute(state_, st.cols, st.off))
           for (size_t i : st.ops) apply_op_to(state_, p.ops[i]);
         break;
+      }
       case ForwardStep::Op:
         apply_op_to(state_, p.ops[st.ops[0]]);
         break;
@@ -932,7 +996,11 @@ void Simulator::sweep_fused(const Circuit &c) {
         break;
       }
       case BackwardStep::PermuteUndo:
-        if (permute(state_, st.cols, st.off)) {
+        if (restore_checkpoint(st.cols, st.off)) {
+          // the state from the forward pass's checkpoint; the co-state gathered
+          if (!permute(costate_, st.cols, st.off))
+            for (size_t k : st.gates) apply_gate_to(costate_, invert(c.ops[k]));
+        } else if (permute(state_, st.cols, st.off)) {
           if (!permute(costate_, st.cols, st.off))
             throw std::runtime_error("permutation: scratch buffer lost");
         } else {
@@ -958,11 +1026,18 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
     // reference's algorithm (fused = false) runs the forward gate by gate, as
     // src/metal/simulator.mm:840-845 does.
     reset();
-    if (fused) run_merged(build_plan(c, FusionOptions{}));
-    else run(build_plan(c, FusionOptions::none()));
+    drop_checkpoints();
+    if (fused) {
+      keep_ckpts_ = true;
+      run_merged(build_plan(c, FusionOptions{}));
+      keep_ckpts_ = false;
+    } else {
+      run(build_plan(c, FusionOptions::none()));
+    }
     if (fused) {
       energy_and_costate(h);
       sweep_fused(c);
+      drop_checkpoints();
     } else {
       // The reference's co-state: one pass per flip mask, then the energy.
       costate(h);
@@ -977,6 +1052,8 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
     fetch(1, true);
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
+    keep_ckpts_ = false;
+    drop_checkpoints();
     throw;
   }
   return {h_results_[0], grad};
@@ -993,10 +1070,14 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
   prepare_adjoint(c, h);
   try {
     reset();
+    drop_checkpoints();
+    keep_ckpts_ = true;
     run_merged(build_plan(c, FusionOptions{}));
+    keep_ckpts_ = false;
     if (shots) launch_sample(shots, seed);
     energy_and_costate(h);
     sweep_fused(c);
+    drop_checkpoints();
     if (!c.ops.empty() && grad)
       cuda_check(cudaMemcpyAsync(grad, d_grad_, c.ops.size() * sizeof(double),
                                  cudaMemcpyDeviceToHost, S(stream_)),
@@ -1008,6 +1089,8 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
     fetch(1, true);
   } catch (...) {
     cudaStreamSynchronize(S(stream_));
+    keep_ckpts_ = false;
+    drop_checkpoints();
     throw;
   }
   if (energy) *energy = h_results_[0];

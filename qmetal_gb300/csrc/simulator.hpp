@@ -135,6 +135,20 @@ class Simulator {
   // buf <- buf gathered through the affine map (cols, off); buf then names
   // the gathered buffer and the old one becomes the scratch.
   bool permute(float *&buf, const std::vector<uint64_t> &cols, uint64_t off);
+  // State checkpoints at permutation passes. A gradient's forward pass keeps
+  // the state from before each CX / SWAP run it gathers (the gather is out
+  // of place, so that state is already in a buffer of its own) while spare
+  // buffers fit on the device; the backward sweep then restores the state
+  // from the checkpoint instead of gathering it back, and gathers only the
+  // co-state. Buffers stay with the simulator for its next gradient.
+  struct Checkpoint {
+    float *buf;                  // the state before the forward gather
+    std::vector<uint64_t> cols;  // that gather's map
+    uint64_t off;
+  };
+  float *take_buffer();
+  void drop_checkpoints();
+  bool restore_checkpoint(const std::vector<uint64_t> &cols, uint64_t off);
   void invalidate_graphs();
 
   uint32_t n_ = 0;
@@ -168,6 +182,9 @@ class Simulator {
   };
   std::vector<GraphEntry> graphs_;   // most recent last
   bool fault_launch_ = false;
+  std::vector<Checkpoint> ckpts_;   // last on top
+  std::vector<float *> ck_free_;    // state-sized buffers not in use
+  bool keep_ckpts_ = false;         // run_merged keeps checkpoints (gradient forward passes)
 };
 
 }  // namespace qmetal
