@@ -140,6 +140,10 @@ Simulator::Simulator(uint32_t n) : n_(n) {
     reset();
     // An injected launch fault affects calls after construction only.
     fault_launch_ = fault && std::strcmp(fault, "launch") == 0;
+    // Tests cap the state checkpoints to drive the paths where only some
+    // of a gradient's gathers can keep one.
+    if (const char *cap = std::getenv("QMETAL_MAX_CHECKPOINTS"))
+      ck_limit_ = static_cast<size_t>(std::strtoul(cap, nullptr, 10));
   } catch (...) {
     release();
     throw;
@@ -228,8 +232,9 @@ float *Simulator::take_buffer() {
     ck_free_.pop_back();
     return b;
   }
-  constexpr size_t kMaxBuffers = 16;
-  if (ckpts_.size() >= kMaxBuffers) return nullptr;
+  size_t held = 0;
+  for (const Checkpoint &c : ckpts_) held += c.buf != nullptr;
+  if (held >= ck_limit_) return nullptr;
   const size_t bytes = dim() * 8;
   size_t free_b = 0, total_b = 0;
   float *b = nullptr;
@@ -243,29 +248,70 @@ float *Simulator::take_buffer() {
 }
 
 void Simulator::drop_checkpoints() {
-  for (const Checkpoint &c : ckpts_) ck_free_.push_back(c.buf);
+  for (const Checkpoint &c : ckpts_)
+    if (c.buf) ck_free_.push_back(c.buf);
   ckpts_.clear();
 }
 
-// The top checkpoint, if the undo gather (cols, off) inverts the forward
-// gather it was taken at: dst1[y] = src[A y ^ a], dst2[z] = dst1[B z ^ b]
-// is the identity when A B = I and A b ^ a = 0.
-bool Simulator::restore_checkpoint(const std::vector<uint64_t> &cols, uint64_t off) {
-  if (ckpts_.empty()) return false;
-  const Checkpoint &c = ckpts_.back();
-  if (c.cols.size() != n_ || cols.size() != n_) return false;
+namespace {
+
+// Does the undo gather (b, boff) invert the forward gather (a, aoff)?
+// dst1[y] = src[A y ^ a], dst2[z] = dst1[B z ^ b] is the identity when
+// A B = I and A b ^ a = 0.
+bool inverts(uint32_t n, const std::vector<uint64_t> &a, uint64_t aoff,
+             const std::vector<uint64_t> &b, uint64_t boff) {
+  if (a.size() != n || b.size() != n) return false;
   auto apply = [&](uint64_t x) {
     uint64_t y = 0;
-    for (uint32_t k = 0; k < n_; k++)
-      if ((x >> k) & 1ull) y ^= c.cols[k];
+    for (uint32_t k = 0; k < n; k++)
+      if ((x >> k) & 1ull) y ^= a[k];
     return y;
   };
-  for (uint32_t j = 0; j < n_; j++)
-    if (apply(cols[j]) != (1ull << j)) return false;
-  if ((apply(off) ^ c.off) != 0) return false;
+  for (uint32_t j = 0; j < n; j++)
+    if (apply(b[j]) != (1ull << j)) return false;
+  return (apply(boff) ^ aoff) == 0;
+}
+
+}  // namespace
+
+// The forward schedule's gathers, last first, against the backward
+// schedule's undo gathers in the order the sweep meets them: the same
+// number, each undoing its partner, and no CX or SWAP undone one gate at a
+// time (which would leave a forward gather without its partner).
+bool Simulator::checkpoints_pair(const Circuit &c, const Plan &p) const {
+  std::vector<const ForwardStep *> fwd;
+  const auto fs = merged_schedule(p);
+  for (const ForwardStep &st : fs)
+    if (st.kind == ForwardStep::Permute) fwd.push_back(&st);
+  if (fwd.empty()) return false;
+  size_t i = fwd.size();
+  for (const BackwardStep &st : backward_schedule(c, tile_high_)) {
+    if (st.kind == BackwardStep::GateUndo) {
+      const GateKind k = c.ops[st.gates[0]].kind;
+      if (k == G_CX || k == G_SWAP) return false;
+    } else if (st.kind == BackwardStep::PermuteUndo) {
+      if (i == 0) return false;
+      --i;
+      if (!inverts(n_, fwd[i]->cols, fwd[i]->off, st.cols, st.off)) return false;
+    }
+  }
+  return i == 0;
+}
+
+// The top checkpoint, paired with this undo gather by checkpoints_pair:
+// restores the state from it when it holds a buffer.
+bool Simulator::restore_checkpoint(const std::vector<uint64_t> &cols, uint64_t off) {
+  if (ckpts_.empty()) return false;
+  const Checkpoint c = ckpts_.back();
+  ckpts_.pop_back();
+  if (!c.buf) return false;
+  if (!inverts(n_, c.cols, c.off, cols, off)) {   // pairing broke: keep nothing more
+    ck_free_.push_back(c.buf);
+    drop_checkpoints();
+    return false;
+  }
   ck_free_.push_back(state_);
   state_ = c.buf;
-  ckpts_.pop_back();
   invalidate_graphs();   // captured graphs hold the old state pointer
   return true;
 }
@@ -464,6 +510,7 @@ void Simulator::run_merged(const Plan &p) {
             break;
           }
         }
+        if (keep_ckpts_) ckpts_.push_back({nullptr, st.cols, st.off});   // keeps the pairing
         if (!permute(state_, st.cols, st.off))
           for (size_t i : st.ops) apply_op_to(state_, p.ops[i]);
         break;
@@ -1028,8 +1075,9 @@ std::pair<double, std::vector<double>> Simulator::energy_and_gradient(const Circ
     reset();
     drop_checkpoints();
     if (fused) {
-      keep_ckpts_ = true;
-      run_merged(build_plan(c, FusionOptions{}));
+      const Plan plan = build_plan(c, FusionOptions{});
+      keep_ckpts_ = checkpoints_pair(c, plan);
+      run_merged(plan);
       keep_ckpts_ = false;
     } else {
       run(build_plan(c, FusionOptions::none()));
@@ -1071,8 +1119,9 @@ void Simulator::serve(const Circuit &c, const Hamiltonian &h, size_t shots, uint
   try {
     reset();
     drop_checkpoints();
-    keep_ckpts_ = true;
-    run_merged(build_plan(c, FusionOptions{}));
+    const Plan plan = build_plan(c, FusionOptions{});
+    keep_ckpts_ = checkpoints_pair(c, plan);
+    run_merged(plan);
     keep_ckpts_ = false;
     if (shots) launch_sample(shots, seed);
     energy_and_costate(h);

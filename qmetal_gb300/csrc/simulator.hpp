@@ -141,13 +141,18 @@ class Simulator {
   // buffers fit on the device; the backward sweep then restores the state
   // from the checkpoint instead of gathering it back, and gathers only the
   // co-state. Buffers stay with the simulator for its next gradient.
+  // Checkpoints are kept only when the forward schedule's gathers and the
+  // backward schedule's undo gathers pair up one to one in reverse order
+  // (checkpoints_pair); a gather that finds no spare buffer leaves an empty
+  // checkpoint so the positions stay paired.
   struct Checkpoint {
-    float *buf;                  // the state before the forward gather
+    float *buf;                  // the state before the forward gather (null: none kept)
     std::vector<uint64_t> cols;  // that gather's map
     uint64_t off;
   };
   float *take_buffer();
   void drop_checkpoints();
+  bool checkpoints_pair(const Circuit &c, const Plan &p) const;
   bool restore_checkpoint(const std::vector<uint64_t> &cols, uint64_t off);
   void invalidate_graphs();
 
@@ -185,6 +190,7 @@ class Simulator {
   std::vector<Checkpoint> ckpts_;   // last on top
   std::vector<float *> ck_free_;    // state-sized buffers not in use
   bool keep_ckpts_ = false;         // run_merged keeps checkpoints (gradient forward passes)
+  size_t ck_limit_ = 16;            // most checkpoint buffers (QMETAL_MAX_CHECKPOINTS)
 };
 
 }  // namespace qmetal

@@ -625,3 +625,23 @@ def test_block_tiles_every_width(n, tile_high):
     assert np.abs(np.array(g1) - g0).max() <= 1e-5
     e2, g2 = qm.Simulator(n).set_tile_high(4).energy_and_gradient(c, h)
     assert np.abs(np.array(g1) - np.array(g2)).max() <= 1e-5
+
+
+@pytest.mark.parametrize("cap", [0, 1, 3, 16])
+def test_state_checkpoints_any_number(cap, monkeypatch):
+    """The gradient's forward pass keeps the state before each gathered CX
+    ladder while spare buffers allow, and the sweep restores it instead of
+    gathering it back. With room for none, some or all of them (the cap
+    stands in for a device that is nearly full: at 33 qubits one fits), the
+    gradient is the oracle's: a checkpoint is only ever restored at the undo
+    it was taken for, even though every layer's ladder is the same map."""
+    monkeypatch.setenv("QMETAL_MAX_CHECKPOINTS", str(cap))
+    n = 14
+    gates, terms = W.hea_gradient_problem(n, depth=6, seed=7)
+    sim = qm.Simulator(n)
+    e, g = sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+    e0, g0 = oracle.energy_and_gradient(n, gates, terms)
+    assert abs(e - e0) <= 1e-5
+    assert np.abs(np.array(g) - g0).max() <= 1e-5
+    e1, g1 = sim.energy_and_gradient(W.to_circuit(n, gates), W.to_hamiltonian(terms))
+    assert np.abs(np.array(g1) - g0).max() <= 1e-5
