@@ -274,6 +274,20 @@ struct BlkGroupArgs {
   M2 m0;             // wire 0 when W0
 };
 
+__device__ __forceinline__ void cp_async16(void *smem, const void *gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(
+                   static_cast<uint32_t>(__cvta_generic_to_shared(smem))),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_group 0;" ::: "memory"); }
+
+// Blocks loop over sites. Each thread copies its next site's sixteen vectors
+// into its own first-layout slots (16-byte cp.async, waited for by the
+// thread that issued them) once every warp of the site has read the current
+// second layout, so the copies overlap the second half of the arithmetic and
+// the stores.
 template <int WB, bool W0, int CLS>
 __global__ void __launch_bounds__(kThreads, 2)
 k_group_blk(float4 *__restrict__ st, uint64_t nsites, BlkGroupArgs g) {
@@ -287,8 +301,8 @@ k_group_blk(float4 *__restrict__ st, uint64_t nsites, BlkGroupArgs g) {
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t sib = warp / NW, wsl = warp % NW;
   float4 *site = xq + static_cast<size_t>(sib) * ROWS * 32;
-  const uint64_t sidx = static_cast<uint64_t>(blockIdx.x) * SPB + sib;
-  const bool active = sidx < nsites;   // uniform over the site's warps
+  const uint64_t per_round = static_cast<uint64_t>(gridDim.x) * SPB;
+  const uint64_t rounds = (nsites + per_round - 1) / per_round;
   // Rows in the first layout (register bits = wires 0..3 of the group, warp
   // bits = wires 4..) and the second (register bits = wires 4.., then wires
   // WB..3; warp bits = wires 0..WB-1); each warp's offsets worked out once.
@@ -308,22 +322,33 @@ k_group_blk(float4 *__restrict__ st, uint64_t nsites, BlkGroupArgs g) {
     row_off[warp][lane / NV][l] = v;
   }
   __syncwarp();
-  uint64_t base = sidx * 32 + lane;
+  auto site_of = [&](uint64_t r) {
+    return r * per_round + static_cast<uint64_t>(blockIdx.x) * SPB + sib;
+  };
+  auto base_of = [&](uint64_t sidx) {
+    uint64_t b = sidx * 32 + lane;
 #pragma unroll
-  for (int j = 0; j < KB; j++) base = ins0(base, g.pos[j]);
-  float4 r[NV];
-#pragma unroll
-  for (int l = 0; l < NV; l++)
-    r[l] = active ? st[base | row_off[warp][0][l]] : make_float4(0.f, 0.f, 0.f, 0.f);
-  if (W0) {
-#pragma unroll
-    for (int l = 0; l < NV; l++) {
-      float2 x = lo2(r[l]), y = hi2(r[l]);
-      apply2c(CLS, g.m0, x, y);
-      r[l] = pack4(x, y);
+    for (int j = 0; j < KB; j++) b = ins0(b, g.pos[j]);
+    return b;
+  };
+  auto site_sync = [&]() {
+    if constexpr (SPB == 1) {
+      __syncthreads();
+    } else {
+      asm volatile("bar.sync %0, %1;" ::"r"(sib + 1), "r"(NW * 32) : "memory");
     }
-  }
-  auto reg_wire = [&](int j, const M2 &m) {
+  };
+  auto prefetch = [&](uint64_t r) {
+    const uint64_t sidx = site_of(r);
+    if (r < rounds && sidx < nsites) {
+      const uint64_t base = base_of(sidx);
+#pragma unroll
+      for (int l = 0; l < NV; l++)
+        cp_async16(site + row_a(l) * 32 + lane, st + (base | row_off[warp][0][l]));
+    }
+    cp_async_commit();
+  };
+  auto reg_wire = [&](float4 (&r)[NV], int j, const M2 &m) {
 #pragma unroll
     for (int l = 0; l < NV; l++) {
       if ((l >> j) & 1) continue;
@@ -335,23 +360,44 @@ k_group_blk(float4 *__restrict__ st, uint64_t nsites, BlkGroupArgs g) {
       r[h] = pack4(b0, b1);
     }
   };
+  prefetch(0);
+  for (uint64_t rd = 0; rd < rounds; rd++) {
+    const uint64_t sidx = site_of(rd);
+    const bool active = sidx < nsites;   // uniform over the site's warps
+    float4 r[NV];
+    cp_async_wait_all();                 // this thread's copies of this round
+    if (active) {
 #pragma unroll
-  for (int j = 0; j < 4; j++) reg_wire(j, g.m[j]);
+      for (int l = 0; l < NV; l++) r[l] = site[row_a(l) * 32 + lane];
+      if (W0) {
 #pragma unroll
-  for (int l = 0; l < NV; l++) site[row_a(l) * 32 + lane] = r[l];
-  if constexpr (SPB == 1) {
-    __syncthreads();
-  } else {
-    asm volatile("bar.sync %0, %1;" ::"r"(sib + 1), "r"(NW * 32) : "memory");
+        for (int l = 0; l < NV; l++) {
+          float2 x = lo2(r[l]), y = hi2(r[l]);
+          apply2c(CLS, g.m0, x, y);
+          r[l] = pack4(x, y);
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; j++) reg_wire(r, j, g.m[j]);
+#pragma unroll
+      for (int l = 0; l < NV; l++) site[row_a(l) * 32 + lane] = r[l];
+    }
+    site_sync();   // the first layout is written back
+    if (active) {
+#pragma unroll
+      for (int l = 0; l < NV; l++) r[l] = site[row_b(l) * 32 + lane];
+    }
+    site_sync();   // every warp has read its second layout: the slots are free
+    prefetch(rd + 1);
+    if (active) {
+#pragma unroll
+      for (int j = 0; j < WB; j++) reg_wire(r, j, g.m[4 + j]);
+      const uint64_t base = base_of(sidx);
+#pragma unroll
+      for (int l = 0; l < NV; l++) st[base | row_off[warp][1][l]] = r[l];
+    }
   }
-#pragma unroll
-  for (int l = 0; l < NV; l++) r[l] = site[row_b(l) * 32 + lane];
-#pragma unroll
-  for (int j = 0; j < WB; j++) reg_wire(j, g.m[4 + j]);
-  if (active) {
-#pragma unroll
-    for (int l = 0; l < NV; l++) st[base | row_off[warp][1][l]] = r[l];
-  }
+  cp_async_wait_all();
 }
 
 struct WarpGroupArgs {
@@ -765,7 +811,10 @@ static int launch_group_blk_cls(float4 *st, uint64_t nsites, const BlkGroupArgs 
     if (e != cudaSuccess) return static_cast<int>(e);
     opted[dev] = true;
   }
-  k_group_blk<WB, W0, CLS><<<grid_for(nsites, SPB), kThreads, smem, s>>>(st, nsites, g);
+  // Resident blocks only: each loops over its sites.
+  const unsigned grid = std::min<unsigned>(grid_for(nsites, SPB),
+                                           static_cast<unsigned>(qmk_host::num_sms()) * 2);
+  k_group_blk<WB, W0, CLS><<<grid, kThreads, smem, s>>>(st, nsites, g);
   return launch_status();
 }
 
