@@ -48,12 +48,13 @@ N_QUBITS = 30
 N_CPU = 20
 OP_NAMES = ["dense1q", "group", "blocked", "controlled1q", "diagonal", "swap", "ccx"]
 # DRAM bytes (read + write) per algorithmic byte of one launch, from ncu's
-# dram__bytes_read.sum + dram__bytes_write.sum on single launches at 26 qubits
-# (k_group<4,0>: 536.9 + 475.8 MB; k_diag: 537.0 + 477.4 MB; 2S = 1073.7 MB
-# each). The traffic grows with the state, so a launch at n qubits is charged
-# this fraction of its 2S.
-DRAM_PER_ALGO_BYTE = {1: (536.9 + 475.8) / 1073.7, 4: (537.0 + 477.4) / 1073.7}
-DRAM_CAPTURE_QUBITS = 26
+# dram__bytes_read.sum + dram__bytes_write.sum on single launches: the group
+# kernel at 28 qubits (k_group<4,0,2>: 2147.5 + 2085.9 MB against 2S =
+# 4295.0 MB), the diagonal layer at 26 (k_diag: 537.0 + 477.4 MB against
+# 1073.7 MB). The traffic grows with the state, so a launch at n qubits is
+# charged this fraction of its 2S.
+DRAM_PER_ALGO_BYTE = {1: (2147.5 + 2085.9) / 4295.0, 4: (537.0 + 477.4) / 1073.7}
+DRAM_CAPTURE_QUBITS = {1: 28, 4: 26}
 OP_STATE_PASSES = {0: 2.0, 1: 2.0, 2: 2.0, 3: 1.0, 4: 2.0, 5: 1.0, 6: 0.5}  # x S
 
 
@@ -934,9 +935,10 @@ def main():
                          "peak_source": peak_src,
                          "traffic": (round(DRAM_PER_ALGO_BYTE[dom] * op_bytes(dom, n))
                                      if dom in DRAM_PER_ALGO_BYTE else None),
-                         "traffic_source": f"ncu dram bytes per launch at "
-                                           f"n={DRAM_CAPTURE_QUBITS}, scaled by units to "
-                                           f"n={n}"},
+                         "traffic_source": (f"ncu dram bytes per launch at "
+                                            f"n={DRAM_CAPTURE_QUBITS[dom]}, scaled by units "
+                                            f"to n={n}") if dom in DRAM_CAPTURE_QUBITS
+                                           else None},
             "kernels": breakdown,
             "frac_of_peak_overall": round(value / world / peak, 4),
             "e2e": {"value": round(e2e_value, 2), "unit": "GB/s", "h2d_bytes_per_step": h2d,
