@@ -435,16 +435,21 @@ def test_costate_schedule_edge_cases():
     assert all(s[0] != "local" for s in steps)
 
 
-@pytest.mark.parametrize("name,widest", [("hea13", 5), ("hea14", 6), ("maxcut16", 6)])
-def test_block_tiles_form_for_uniform_layers(name, widest):
-    """Rotation layers past the first tile go five or six wires >= 6 per pass
-    with tile_high 6, and never more than four with tile_high 4."""
+@pytest.mark.parametrize("name", ["hea13", "hea14", "maxcut16"])
+def test_block_tiles_form_for_uniform_layers(name):
+    """Rotation layers go five or six wires >= 6 per pass with tile_high 6,
+    and never more than four with tile_high 4; with block tiles the first
+    tile of a layer (wires 0..5) keeps no more wires >= 6 than leave the
+    number of passes at its least."""
     _, n, gates, _ = next(p for p in PROBLEMS if p[0] == name)
     c = W.to_circuit(n, gates)
-    for th, want in ((6, widest), (4, 4)):
+    passes = {}
+    for th in (6, 4):
         steps = decode_backward(c.schedule_export("backward", tile_high=th))
         high = [len({w for w, _, _, _ in s[1] if w >= 6}) for s in steps if s[0] == "window"]
-        assert max(high) == want, (th, high)
+        assert max(high) >= 5 if th == 6 else max(high) == 4, (th, high)
+        passes[th] = len(high)
+    assert passes[6] <= passes[4]
 
 
 @pytest.mark.parametrize("tile_high", [1, 2, 4, 5, 6])
