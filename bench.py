@@ -301,6 +301,10 @@ def _costate_bytes(flat, S):
             overwrite, nt = int(flat[pos + 1]), int(flat[pos + 3])
             total += (2 if overwrite else 3) * S
             pos += 4 + 3 * nt
+        elif kind == 5:
+            overwrite, nw = int(flat[pos + 1]), int(flat[pos + 3])
+            total += (2 if overwrite else 3) * S
+            pos += 4 + 2 * nw
         else:
             total += (1 if kind == 3 else 2) * S
             pos += 1

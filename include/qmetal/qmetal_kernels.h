@@ -146,6 +146,20 @@ int qmk_pauli_accum_local(float *lambda, const float *psi, uint32_t n,
                           const uint64_t *sign_masks, const uint32_t *ny,
                           const double *coeffs, int overwrite, void *stream);
 
+/* A transverse field: lambda (=|+=) sum_w coeffs[k] X_w psi over distinct
+ * wires w = wires[k] (no Y, no Z signs), any of wires 0..5 and at most seven
+ * wires >= 6, n >= 10: one pass over both states, psi staged through shared
+ * memory. energy 1 writes, 2 adds, sum_k coeffs[k] <psi|X_w|psi> to
+ * *d_energy (0: neither; the workspace is then not used). Refuses repeated
+ * or out-of-range wires. No counterpart in the reference, which builds the
+ * co-state one term per pass and the energy by a separate reduction
+ * (simulator.mm:856-904). */
+int qmk_xfield_costate(float *lambda, const float *psi, uint32_t n,
+                       uint32_t num_wires, const uint32_t *wires,
+                       const double *coeffs, int overwrite, double *d_energy,
+                       int energy, void *workspace, size_t workspace_bytes,
+                       void *stream);
+
 /* Re<a|b> into *d_out. Replaces the host energy loop of simulator.mm:897-904. */
 int qmk_dot_re(const float *a, const float *b, uint32_t n, double *d_out,
                void *workspace, size_t workspace_bytes, void *stream);

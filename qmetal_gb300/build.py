@@ -31,7 +31,8 @@ CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-Wall", "-Wextr
              "-I" + os.path.join(CUDA_HOME, "include")]
 
 CU_SOURCES = ["k_gates.cu", "k_diag.cu", "k_reduce.cu", "k_sample.cu", "k_adjoint.cu",
-              "k_noalloc.cu", "k_perm.cu", "k_adjoint_tiles.cu", "k_adjoint_uniform.cu"]
+              "k_noalloc.cu", "k_perm.cu", "k_adjoint_tiles.cu", "k_adjoint_uniform.cu",
+              "k_xfield.cu"]
 CXX_SOURCES = ["circuit.cpp", "plan.cpp", "schedule.cpp", "simulator.cpp", "batch.cpp", "capi.cpp"]
 HEADERS = ["kcommon.cuh", "kquad.cuh", "kreduce.cuh", "kadjoint.cuh", "kadjoint_ops.cuh",
            "circuit.hpp", "schedule.hpp",

@@ -233,23 +233,25 @@ std::vector<FlipGroup> group_by_flip(const std::vector<const PauliTerm *> &terms
 
 }  // namespace
 
-// Z strings of <= 2 bits go as one quadratic-form pass; terms that flip one
-// wire pack many wires per pass (wires 0..5 ride along in every pass, at most
+// Z strings of <= 2 bits go as one quadratic-form pass; plain X_w terms
+// (a transverse field) go as block passes of up to seven wires >= 6 with any
+// of wires 0..5, the terms on one wire summed; other terms that flip one wire
+// pack many wires per pass (wires 0..5 ride along in every pass, at most
 // four wires >= 6 and 16 terms a pass); anything else goes one pass per flip
-// mask, 16 terms at a time. A Hamiltonian of only short Z strings needs no
-// separate energy pass.
+// mask, 16 terms at a time. When every term is of the first two kinds their
+// passes also sum the energy, and no separate energy pass follows.
 std::vector<CostateStep> costate_schedule(const Hamiltonian &h, uint32_t n) {
   std::vector<CostateStep> out;
-  bool zonly = !h.terms.empty();
-  for (const PauliTerm &t : h.terms)
-    if (t.pauli.x_mask | t.pauli.y_mask || popc(t.pauli.z_mask) > 2) zonly = false;
-  std::vector<const PauliTerm *> zpart, local, rest;
+  std::vector<const PauliTerm *> zpart, xfield, local, rest;
   for (const PauliTerm &t : h.terms) {
     const uint64_t flip = t.pauli.x_mask | t.pauli.y_mask;
     if (!flip && popc(t.pauli.z_mask) <= 2) zpart.push_back(&t);
+    else if (popc(flip) == 1 && !t.pauli.y_mask && !t.pauli.z_mask && n >= kXFieldMinQubits)
+      xfield.push_back(&t);
     else if (popc(flip) == 1 && n >= 6) local.push_back(&t);
     else rest.push_back(&t);
   }
+  const bool fused_energy = local.empty() && rest.empty() && !h.terms.empty();
   bool first = true;
   if (!zpart.empty()) {
     CostateStep s;
@@ -261,8 +263,38 @@ std::vector<CostateStep> costate_schedule(const Hamiltonian &h, uint32_t n) {
     }
     out.push_back(std::move(s));
     first = false;
-    if (zonly) return out;
   }
+  if (!xfield.empty()) {
+    std::map<uint32_t, double> coef;   // wire -> summed coefficient, ascending
+    for (const PauliTerm *t : xfield)
+      coef[static_cast<uint32_t>(__builtin_ctzll(t->pauli.x_mask))] += t->coefficient;
+    std::vector<uint32_t> low, high;
+    for (const auto &wc : coef) (wc.first < 6 ? low : high).push_back(wc.first);
+    // ceil(H / 7) passes, as even as possible (22 wires: 6, 6, 5, 5); wires
+    // 0..5 join the last, which is among the smallest.
+    const size_t passes = std::max<size_t>(
+        1, (high.size() + kXFieldHighPerPass - 1) / kXFieldHighPerPass);
+    size_t at = 0;
+    for (size_t p = 0; p < passes; p++) {
+      const size_t take = high.size() / passes + (p < high.size() % passes ? 1 : 0);
+      CostateStep s;
+      s.kind = CostateStep::XField;
+      s.overwrite = first;
+      if (fused_energy) s.energy = first ? 1 : 2;
+      first = false;
+      if (p + 1 == passes)
+        for (uint32_t w : low) {
+          s.wires.push_back(w);
+          s.coeffs.push_back(coef[w]);
+        }
+      for (size_t j = 0; j < take; j++, at++) {
+        s.wires.push_back(high[at]);
+        s.coeffs.push_back(coef[high[at]]);
+      }
+      out.push_back(std::move(s));
+    }
+  }
+  if (fused_energy) return out;
   if (!local.empty()) {
     auto wire_of = [&](const PauliTerm *t) {
       return static_cast<uint32_t>(__builtin_ctzll(t->pauli.x_mask | t->pauli.y_mask));
@@ -723,6 +755,15 @@ void serialise_schedule(const std::vector<CostateStep> &s, std::vector<double> &
         for (size_t i = 0; i < st.masks.size(); i++) {
           v.push_back(static_cast<double>(st.masks[i]));
           v.push_back(st.nys[i]);
+          v.push_back(st.coeffs[i]);
+        }
+        break;
+      case CostateStep::XField:
+        v.push_back(st.overwrite ? 1.0 : 0.0);
+        v.push_back(st.energy);
+        v.push_back(static_cast<double>(st.wires.size()));
+        for (size_t i = 0; i < st.wires.size(); i++) {
+          v.push_back(st.wires[i]);
           v.push_back(st.coeffs[i]);
         }
         break;

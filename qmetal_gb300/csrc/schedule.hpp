@@ -71,11 +71,13 @@ struct CostateStep {
     Flip,    // terms sharing one flip mask: lambda (+)= sum c_t P_t psi
     Zero,    // lambda = 0 (no terms)
     Dot,     // energy = Re <psi | lambda>
+    XField,  // terms c_w X_w, one per wire: lambda (+)= sum c_w X_w psi
   };
   Kind kind = Zero;
-  bool overwrite = false;        // Local / Flip: first write of lambda
+  bool overwrite = false;        // Local / Flip / XField: first write of lambda
+  uint8_t energy = 0;            // XField: 1 writes, 2 adds sum c_w <psi|X_w|psi> to the energy
   uint64_t flip = 0;             // Flip
-  std::vector<uint32_t> wires;   // Local: the wire each term flips
+  std::vector<uint32_t> wires;   // Local / XField: the wire each term flips
   std::vector<uint64_t> masks;   // ZDiag: Z masks; Local / Flip: sign masks (y | z)
   std::vector<uint32_t> nys;     // Local / Flip: Y count of each term
   std::vector<double> coeffs;
@@ -83,6 +85,10 @@ struct CostateStep {
 
 // Terms per Flip / Local pass.
 constexpr uint32_t kCostateTermsPerPass = 16;
+// Wires >= 6 per XField pass (any of wires 0..5 ride along), and the least
+// width it serves (a pass holds at least four wires >= 6).
+constexpr uint32_t kXFieldHighPerPass = 7;
+constexpr uint32_t kXFieldMinQubits = 10;
 
 std::vector<CostateStep> costate_schedule(const Hamiltonian &h, uint32_t n);
 

@@ -968,6 +968,13 @@ double Simulator::energy_and_costate(const Hamiltonian &h) {
               "co-state");
         dispatches_++;
         break;
+      case CostateStep::XField:
+        check(qmk_xfield_costate(costate_, state_, n_, nt, st.wires.data(), st.coeffs.data(),
+                                 st.overwrite ? 1 : 0, d_results_, st.energy, ws_, ws_bytes_,
+                                 stream_),
+              "co-state");
+        dispatches_++;
+        break;
       case CostateStep::Zero:
         cuda_check(cudaMemsetAsync(costate_, 0, dim() * 8, S(stream_)), "co-state zero");
         break;

@@ -199,3 +199,84 @@ def test_local_costate_terms(n):
         lam = torch.zeros_like(p)
         assert f(lam.data_ptr(), p.data_ptr(), n, 5, wires.ctypes.data, z.ctypes.data,
                  zi.ctypes.data, c1.ctypes.data, 1, None) != 0
+
+
+@pytest.mark.parametrize("n", [10, 11, 12, 14, 17])
+def test_xfield_costate(n):
+    """qmk_xfield_costate: a transverse field on any of wires 0..5 and up to
+    seven wires >= 6 per pass (sites of four to seven wires, padded with
+    wires of coefficient 0), overwriting and accumulating lambda, with the
+    energy left alone, written or added, against complex128."""
+    torch = pytest.importorskip("torch")
+    from ctypes import c_double, c_size_t
+    L = ctypes.CDLL(qm.library_path())
+    f = L.qmk_xfield_costate
+    f.restype = c_int
+    f.argtypes = [c_void_p, c_void_p, c_uint32, c_uint32, c_void_p, c_void_p, c_int, c_void_p,
+                  c_int, c_void_p, c_size_t, c_void_p]
+    L.qmk_workspace_bytes.restype = c_size_t
+    L.qmk_workspace_bytes.argtypes = [c_uint32]
+    wsb = L.qmk_workspace_bytes(n)
+    ws = torch.zeros(wsb, dtype=torch.uint8, device="cuda")
+    rng = np.random.default_rng(400 + n)
+    psi = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    psi /= np.linalg.norm(psi)
+    lam0 = rng.normal(size=1 << n) + 1j * rng.normal(size=1 << n)
+    idx = np.arange(1 << n)
+
+    def dev(z):
+        h = np.empty(2 << n, dtype=np.float32)
+        h[0::2], h[1::2] = z.real, z.imag
+        return torch.from_numpy(h).cuda()
+
+    p = dev(psi)
+    for trial in range(10):
+        low = sorted(rng.choice(6, int(rng.integers(0, 7)), replace=False).tolist())
+        k = int(rng.integers(0, min(7, n - 6) + 1))
+        if trial == 0:
+            low, k = list(range(6)), min(7, n - 6)
+        high = sorted(rng.choice(np.arange(6, n), k, replace=False).tolist())
+        wires = low + high
+        if not wires:
+            continue
+        rng.shuffle(wires)
+        coeffs = rng.uniform(-1, 1, len(wires))
+        overwrite = trial % 2
+        mode = trial % 3
+        part = np.zeros(1 << n, dtype=complex)
+        for w, c in zip(wires, coeffs):
+            part += c * psi[idx ^ (1 << w)]
+        want = part + (0 if overwrite else lam0)
+        e_part = float(np.vdot(psi, part).real)
+        lam = dev(lam0)
+        d_e = torch.full((1,), 0.25, dtype=torch.float64, device="cuda")
+        wa = np.array(wires, dtype=np.uint32)
+        ca = np.array(coeffs, dtype=np.float64)
+        rc = f(lam.data_ptr(), p.data_ptr(), n, len(wires), wa.ctypes.data, ca.ctypes.data,
+               overwrite, d_e.data_ptr(), mode, ws.data_ptr(), wsb, None)
+        assert rc == 0, (n, wires)
+        torch.cuda.synchronize()
+        out = lam.cpu().numpy()
+        got = out[0::2].astype(np.float64) + 1j * out[1::2]
+        assert np.abs(got - want).max() <= 1e-5, (n, trial, wires)
+        e = float(d_e.cpu()[0])
+        expect = {0: 0.25, 1: e_part, 2: 0.25 + e_part}[mode]
+        assert abs(e - expect) <= 1e-5, (n, trial, mode)
+    # refused before any launch: repeated, out-of-range or too many wires,
+    # too narrow a state, an energy without a workspace
+    lam = dev(lam0)
+    d_e = torch.zeros(1, dtype=torch.float64, device="cuda")
+    bad = [([3, 3], n), ([6, 6], n), ([n], n), (list(range(6, 14)), max(n, 14))]
+    for wires, width in bad:
+        if width != n:
+            continue
+        wa = np.array(wires, dtype=np.uint32)
+        ca = np.ones(len(wires))
+        assert f(lam.data_ptr(), p.data_ptr(), n, len(wires), wa.ctypes.data, ca.ctypes.data,
+                 1, d_e.data_ptr(), 1, ws.data_ptr(), wsb, None) != 0, wires
+    wa = np.array([0, 6], dtype=np.uint32)
+    ca = np.ones(2)
+    assert f(lam.data_ptr(), p.data_ptr(), 9, 2, wa.ctypes.data, ca.ctypes.data, 1,
+             d_e.data_ptr(), 1, ws.data_ptr(), wsb, None) != 0
+    assert f(lam.data_ptr(), p.data_ptr(), n, 2, wa.ctypes.data, ca.ctypes.data, 1,
+             d_e.data_ptr(), 1, None, 0, None) != 0

@@ -141,6 +141,9 @@ def decode_costate(v):
         elif kind == 2:
             ow, flip = bool(r.i()), r.i()
             out.append(("flip", ow, flip, [(r.i(), r.i(), r.f()) for _ in range(r.i())]))
+        elif kind == 5:
+            ow, energy = bool(r.i()), r.i()
+            out.append(("xfield", ow, energy, [(r.i(), r.f()) for _ in range(r.i())]))
         else:
             assert kind in (3, 4)
             out.append(("zero",) if kind == 3 else ("dot",))
@@ -203,11 +206,16 @@ def replay_forward(n, gates):
 
 
 def replay_costate(n, psi, terms):
+    """lambda = H psi by the co-state schedule, in complex128; the energy as
+    the passes that carry it sum it (the ZZ pass, then each transverse-field
+    pass's sum_w c_w <psi|X_w|psi>), or by the final dot. Returns lambda, the
+    covered (coefficient, flip, sign, ny) terms and that energy."""
     h = W.to_hamiltonian(terms)
     steps = decode_costate(W.to_circuit(n, []).schedule_export("costate", h))
     lam = None
     covered = []
-    assert steps[-1][0] in ("dot", "zdiag")
+    energy = None
+    assert steps[-1][0] in ("dot", "zdiag", "xfield")
     for k, s in enumerate(steps):
         if s[0] == "zdiag":
             assert k == 0 and lam is None
@@ -216,6 +224,25 @@ def replay_costate(n, psi, terms):
                 assert bin(z).count("1") <= 2
                 lam += c * pauli_apply(psi, n, 0, 0, z)
                 covered.append((c, 0, z))
+            energy = float(np.vdot(psi, lam).real)
+        elif s[0] == "xfield":
+            ow, emode, items = s[1], s[2], s[3]
+            assert ow == (lam is None)
+            if lam is None:
+                lam = np.zeros_like(psi)
+            wires = [w for w, _ in items]
+            assert len(set(wires)) == len(wires) and n >= 10
+            assert sum(w >= 6 for w in wires) <= 7
+            part = np.zeros_like(psi)
+            for w, c in items:
+                part += c * pauli_apply(psi, n, 1 << w, 0, 0)
+                covered.append((c, 1 << w, 0, 0))
+            lam += part
+            # the pass carries the energy exactly when no dot pass follows
+            assert (emode != 0) == (steps[-1][0] != "dot")
+            if emode:
+                assert (emode == 1) == (energy is None)
+                energy = (energy or 0.0) + float(np.vdot(psi, part).real)
         elif s[0] in ("local", "flip"):
             assert s[1] == (lam is None)   # only the first accumulation overwrites
             if lam is None:
@@ -240,7 +267,29 @@ def replay_costate(n, psi, terms):
             lam = np.zeros_like(psi)
         else:
             assert k == len(steps) - 1
-    return lam, covered
+            energy = float(np.vdot(psi, lam).real)
+    return lam, covered, energy
+
+
+def assert_covers(covered, terms):
+    """Every term once: coefficients summed per (flip, sign, Y count) agree
+    (the transverse-field passes sum the terms on one wire)."""
+    def key(x, y, z):
+        return (x | y, y | z, bin(y).count("1"))
+    want, got = {}, {}
+    for c, x, y, z in terms:
+        want[key(x, y, z)] = want.get(key(x, y, z), 0.0) + c
+    for item in covered:
+        if len(item) == 3:                      # a Z string of the ZZ pass
+            c, _, z = item
+            k = key(0, 0, z)
+        else:
+            c, flip, sign, ny = item
+            k = (flip, sign, ny)
+        got[k] = got.get(k, 0.0) + c
+    assert set(got) == set(want)
+    for k in want:
+        assert abs(got[k] - want[k]) <= 1e-12 * max(1.0, abs(want[k])), k
 
 
 def rotation_kind(minv, gen):
@@ -416,19 +465,50 @@ def test_forward_schedule_gathers_cx_ladders(n):
 @pytest.mark.parametrize("name,n,gates,terms", PROBLEMS, ids=[p[0] for p in PROBLEMS])
 def test_costate_schedule_is_h_psi(name, n, gates, terms):
     psi = oracle.run(n, gates)
-    lam, covered = replay_costate(n, psi, terms)
-    assert np.abs(lam - h_apply(psi, n, terms)).max() < 1e-12
-    assert len(covered) == len(terms)
+    lam, covered, energy = replay_costate(n, psi, terms)
+    want = h_apply(psi, n, terms)
+    assert np.abs(lam - want).max() < 1e-12
+    assert abs(energy - float(np.vdot(psi, want).real)) < 1e-12
+    assert_covers(covered, terms)
 
 
-def test_costate_schedule_edge_cases():
-    n = 8
+def transverse_field(n, hx, wires=None):
+    return [(-hx, 1 << q, 0, 0) for q in (range(n) if wires is None else wires)]
+
+
+@pytest.mark.parametrize("n", [8, 12])
+def test_costate_schedule_edge_cases(n):
     psi = oracle.run(n, W.hea(n, depth=1))
     for terms in ([], [(0.5, 0, 0, 0)], [(1.0, 0, 0, 0b111)], one_flip_terms(n, 5),
-                  [(1.0, 1 << 7, 0, 0)] * 20, random_terms(n, 40, 3)):
-        lam, covered = replay_costate(n, psi, terms)
-        assert np.abs(lam - h_apply(psi, n, terms)).max() < 1e-12, terms[:3]
-        assert len(covered) == len(terms)
+                  [(1.0, 1 << 7, 0, 0)] * 20, random_terms(n, 40, 3),
+                  transverse_field(n, 0.7), transverse_field(n, 0.3, [1, 3, 7]),
+                  transverse_field(n, 0.3, [2]) + transverse_field(n, 0.1, [2]),
+                  W.ring_tfim_hamiltonian(n, 0.7),
+                  W.ring_tfim_hamiltonian(n, 0.7) + [(0.2, 0, 1 << 3, 1)]):
+        lam, covered, energy = replay_costate(n, psi, terms)
+        want = h_apply(psi, n, terms)
+        assert np.abs(lam - want).max() < 1e-12, terms[:3]
+        assert abs(energy - float(np.vdot(psi, want).real)) < 1e-12
+        assert_covers(covered, terms)
+
+
+@pytest.mark.parametrize("n,passes", [(10, 1), (13, 1), (14, 2), (20, 2), (28, 4), (34, 4)])
+def test_transverse_field_passes(n, passes):
+    """A transverse field on every wire: ceil((n - 6) / 7) block passes of
+    as even a size as possible, wires 0..5 riding in the last; with the ZZ
+    ring its passes carry the energy and no dot pass follows."""
+    steps = decode_costate(W.to_circuit(n, []).schedule_export(
+        "costate", W.to_hamiltonian(W.ring_tfim_hamiltonian(n, 0.7))))
+    kinds = [s[0] for s in steps]
+    assert kinds == ["zdiag"] + ["xfield"] * passes
+    highs = [sum(w >= 6 for w, _ in s[3]) for s in steps[1:]]
+    assert sum(highs) == n - 6 and max(highs) - min(highs) <= 1 and max(highs) <= 7
+    assert [w for w, _ in steps[-1][3] if w < 6] == list(range(6))
+    assert all(s[2] == 2 and not s[1] for s in steps[1:])
+    # below ten qubits the same field goes by the per-wire tiles
+    small = decode_costate(W.to_circuit(9, []).schedule_export(
+        "costate", W.to_hamiltonian(W.ring_tfim_hamiltonian(9, 0.7))))
+    assert "xfield" not in [s[0] for s in small] and small[-1][0] == "dot"
     # Below 6 qubits one-wire flips go by flip mask.
     steps = decode_costate(W.to_circuit(5, []).schedule_export(
         "costate", W.to_hamiltonian(one_flip_terms(5, 1))))
@@ -553,7 +633,7 @@ def test_random_circuits_replay_property():
         assert np.abs(grad - want).max() < 1e-10
         params = np.array([len(g[2]) > 0 for g in gates])
         assert (touched == params).all()
-        lam, covered = replay_costate(n, oracle.run(n, gates), terms)
+        lam, covered, _ = replay_costate(n, oracle.run(n, gates), terms)
         assert np.abs(lam - h_apply(oracle.run(n, gates), n, terms)).max() < 1e-12
 
     check()
