@@ -2,6 +2,7 @@
 #include "schedule.hpp"
 
 #include <algorithm>
+#include <cstdint>
 #include <map>
 #include <stdexcept>
 
@@ -13,6 +14,20 @@ uint32_t popc(uint64_t x) { return static_cast<uint32_t>(__builtin_popcountll(x)
 constexpr uint32_t kWindowOps = 16;     // ops per window pass below 6 qubits
 constexpr uint32_t kWideWindowOps = 32;  // ops per warp-tile window pass
 constexpr uint32_t kWindowGrads = 16;   // gradients per window pass
+
+// The structure the kernel layer finds in a 2x2 once narrowed to float (the
+// kMat* classes of kcommon.cuh): 3 diagonal, 1 real, 2 RX-like, 0 general.
+int narrowed_class(const cdouble m[4]) {
+  float f[8];
+  for (int k = 0; k < 4; k++) {
+    f[2 * k] = static_cast<float>(m[k].real());
+    f[2 * k + 1] = static_cast<float>(m[k].imag());
+  }
+  if (f[2] == 0.0f && f[3] == 0.0f && f[4] == 0.0f && f[5] == 0.0f) return 3;
+  if (f[1] == 0.0f && f[3] == 0.0f && f[5] == 0.0f && f[7] == 0.0f) return 1;
+  if (f[1] == 0.0f && f[7] == 0.0f && f[2] == 0.0f && f[4] == 0.0f) return 2;
+  return 0;
+}
 
 }  // namespace
 
@@ -119,18 +134,69 @@ std::vector<ForwardStep> merged_schedule(const Plan &p) {
     if (lane == 0 && high >= 6 && high <= 7 && n >= 6 + high) return true;   // block groups
     return lane + high <= 5;
   };
-  auto flush = [&]() {
-    if (wires.empty()) return;
-    std::vector<size_t> order(wires.size());
-    for (size_t i = 0; i < order.size(); i++) order[i] = i;
-    std::sort(order.begin(), order.end(), [&](size_t a, size_t b) { return wires[a] < wires[b]; });
+  // One pass for the given entries of the pending run, wires ascending.
+  auto emit = [&](std::vector<size_t> idx) {
+    if (idx.empty()) return;
+    std::sort(idx.begin(), idx.end(), [&](size_t a, size_t b) { return wires[a] < wires[b]; });
     ForwardStep s;
     s.kind = ForwardStep::Group;
-    for (size_t i : order) {
+    for (size_t i : idx) {
       s.wires.push_back(wires[i]);
       s.mats.insert(s.mats.end(), mats.begin() + 4 * i, mats.begin() + 4 * i + 4);
     }
     out.push_back(std::move(s));
+  };
+  // A run of one-wire ops on distinct wires (they all commute) in the fewest
+  // passes: wires 0..5 take k wires >= 6 along, the rest go up to seven a
+  // pass in order. Where a lane wire's matrix is general, the pass of the
+  // lane wires is bound by its multiply-adds: of the k that give the fewest
+  // passes the least is kept, but at least one where there is one (a pass of
+  // the lane wires alone has too little work per thread to hide its loads),
+  // so an HEA layer at 28 qubits goes as 6 + 1, 7, 7, 7 wires instead of
+  // 6 + 4, 7, 7, 4. Otherwise the greatest is kept.
+  auto flush = [&]() {
+    if (wires.empty()) return;
+    std::vector<size_t> low, high;
+    for (size_t i = 0; i < wires.size(); i++) (wires[i] < 6 ? low : high).push_back(i);
+    auto wires_of = [&](const std::vector<size_t> &idx) {
+      std::vector<uint32_t> w;
+      for (size_t i : idx) w.push_back(wires[i]);
+      return w;
+    };
+    // Wires >= 6 in passes of their own, greedily in order.
+    auto chunks = [&](size_t from) {
+      std::vector<std::vector<size_t>> c;
+      for (size_t j = from; j < high.size(); j++) {
+        if (c.empty()) {
+          c.push_back({high[j]});
+          continue;
+        }
+        std::vector<uint32_t> trial = wires_of(c.back());
+        trial.push_back(wires[high[j]]);
+        if (fits(trial)) c.back().push_back(high[j]);
+        else c.push_back({high[j]});
+      }
+      return c;
+    };
+    // Narrow matrices (real, RX-like, diagonal) halve the lane pass's
+    // multiply-adds: it then keeps as many wires >= 6 as fit.
+    bool general = false;
+    for (size_t i : low) general = general || narrowed_class(&mats[4 * i]) == 0;
+    size_t best_k = 0, best = SIZE_MAX;
+    for (size_t k = low.empty() ? 0 : std::min<size_t>(1, high.size()); k <= high.size(); k++) {
+      std::vector<size_t> first = low;
+      first.insert(first.end(), high.begin(), high.begin() + k);
+      if (!first.empty() && !fits(wires_of(first))) break;
+      const size_t passes = (first.empty() ? 0 : 1) + chunks(k).size();
+      if (passes < best || (!general && passes == best)) {
+        best = passes;
+        best_k = k;
+      }
+    }
+    std::vector<size_t> first = low;
+    first.insert(first.end(), high.begin(), high.begin() + best_k);
+    emit(first);
+    for (const auto &c : chunks(best_k)) emit(c);
     wires.clear();
     mats.clear();
   };
@@ -189,13 +255,9 @@ std::vector<ForwardStep> merged_schedule(const Plan &p) {
     for (uint32_t q : w)
       if (std::find(wires.begin(), wires.end(), q) != wires.end()) overlap = true;
     if (overlap) flush();
-    // The group's wires commute with each other and with the pending ones,
-    // so they join the pass one by one and spill into the next when it is
-    // full.
+    // The group's wires commute with each other and with the pending ones:
+    // they join the pending run, which is split into passes when it ends.
     for (size_t j = 0; j < w.size(); j++) {
-      std::vector<uint32_t> trial = wires;
-      trial.push_back(w[j]);
-      if (!fits(trial)) flush();
       wires.push_back(w[j]);
       mats.insert(mats.end(), m.begin() + 4 * j, m.begin() + 4 * j + 4);
     }
@@ -426,20 +488,6 @@ std::vector<Segment> segment_circuit(const Circuit &c) {
 // block is undone on both states in the same pass. Blocks before the first
 // parameterised one are never undone.
 namespace {
-
-// The structure the kernel layer finds in a 2x2 once narrowed to float (the
-// kMat* classes of kcommon.cuh): 3 diagonal, 1 real, 2 RX-like, 0 general.
-int narrowed_class(const cdouble m[4]) {
-  float f[8];
-  for (int k = 0; k < 4; k++) {
-    f[2 * k] = static_cast<float>(m[k].real());
-    f[2 * k + 1] = static_cast<float>(m[k].imag());
-  }
-  if (f[2] == 0.0f && f[3] == 0.0f && f[4] == 0.0f && f[5] == 0.0f) return 3;
-  if (f[1] == 0.0f && f[3] == 0.0f && f[5] == 0.0f && f[7] == 0.0f) return 1;
-  if (f[1] == 0.0f && f[7] == 0.0f && f[2] == 0.0f && f[4] == 0.0f) return 2;
-  return 0;
-}
 
 // A wire's ops (in undo order) as one of the rotation sequences the block
 // tiles compile in: one RX, RY or RZ, or RZ then RY, or RY then RZ. Returns
