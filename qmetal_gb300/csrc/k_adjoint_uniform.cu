@@ -26,6 +26,15 @@ struct UniArgs {
   uint32_t hpos[6];   // wires >= 6: vector bit - 5, ascending
   uint32_t lbit[5];   // lane wires' vector bits, in op order
   M2 m0[2], ml[5][2], mh[6][2];
+  // Tiles of RZ and RY on every wire: the RZ undos of the register wires
+  // of one layout as one phase per register vector (index l: the product of
+  // a or d of each wire's RZ by bit j of l), for the wires of mh[0..2]
+  // (first layout) and of mh[3..] (second layout of a block tile). In the
+  // tile of wire 0 and wires 1..5, ph[0][2 l + b] also takes wire 0's entry
+  // by amplitude bit b, and lph[lane] is the lane wires' product by the
+  // lane's bits.
+  float2 ph[2][8];
+  float2 lph[32];
 };
 
 // The M ops of one wire: op k has class Ck and generator Gk.
@@ -48,6 +57,76 @@ __device__ __forceinline__ void reg_ops(float4 (&P)[NV], float4 (&L)[NV], const 
                                         float *acc) {
   acc[0] += reg_op<NV, J, C0>(P, L, G0, m[0]);
   if constexpr (M > 1) acc[1] += reg_op<NV, J, C1>(P, L, G1, m[1]);
+}
+
+// The RZ ops of K register wires (bits 0..K-1 of a vector's register
+// index) at once, for tiles with an RZ on every wire. Their gradients need
+// only q = Im(conj(l) p) of each amplitude, which the other wires' RZ phases
+// leave alone and which commutes with the other wires' ops: wire j's
+// overlap is the sum over vectors of +-Q (Q = q of both amplitudes, sign by
+// bit j), as pair by pair in reg_op. Then one phase per vector undoes all K
+// RZs: ph[l] is the product of the wires' diagonal entries picked by l.
+template <int NV, int K>
+__device__ __forceinline__ void rz_block(float4 (&P)[NV], float4 (&L)[NV], const float2 (&ph)[8],
+                                         float *acc, int stride) {
+  float a[K];
+#pragma unroll
+  for (int j = 0; j < K; j++) a[j] = 0.0f;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    const float q = (L[l].x * P[l].y - L[l].y * P[l].x) + (L[l].z * P[l].w - L[l].w * P[l].z);
+#pragma unroll
+    for (int j = 0; j < K; j++) a[j] += ((l >> j) & 1) ? -q : q;
+    const float2 f = ph[l & 7];
+    P[l] = pack4(cmul(f, lo2(P[l])), cmul(f, hi2(P[l])));
+    L[l] = pack4(cmul(f, lo2(L[l])), cmul(f, hi2(L[l])));
+  }
+#pragma unroll
+  for (int j = 0; j < K; j++) acc[j * stride] += a[j];
+}
+
+// The RZ ops of wire 0, the five lane wires and KH register wires at once
+// (the tile of wires 0..5 with an RZ on every wire): wire 0's overlap is
+// q0 - q1 of each vector's two amplitudes, a register wire's +-Q as in
+// rz_block, and a lane wire's the lane's sign times the sum of Q over the
+// thread's vectors (sl; the sign goes on after the last site). One phase per
+// amplitude, lph[lane] ph[2 l + b], undoes them all.
+template <int NV, int KH>
+__device__ __forceinline__ void rz_wide(float4 (&P)[NV], float4 (&L)[NV], const float2 (&ph)[8],
+                                        float2 lp, float &a0, float &sl, float *ar, int stride) {
+  static_assert(NV <= 4, "two register wires at most");
+  float r[KH > 0 ? KH : 1];
+#pragma unroll
+  for (int j = 0; j < KH; j++) r[j] = 0.0f;
+#pragma unroll
+  for (int l = 0; l < NV; l++) {
+    const float q0 = L[l].x * P[l].y - L[l].y * P[l].x;
+    const float q1 = L[l].z * P[l].w - L[l].w * P[l].z;
+    a0 += q0 - q1;
+    const float q = q0 + q1;
+    sl += q;
+#pragma unroll
+    for (int j = 0; j < KH; j++) r[j] += ((l >> j) & 1) ? -q : q;
+    const float2 f0 = cmul(lp, ph[2 * l]), f1 = cmul(lp, ph[2 * l + 1]);
+    P[l] = pack4(cmul(f0, lo2(P[l])), cmul(f1, hi2(P[l])));
+    L[l] = pack4(cmul(f0, lo2(L[l])), cmul(f1, hi2(L[l])));
+  }
+#pragma unroll
+  for (int j = 0; j < KH; j++) ar[j * stride] += r[j];
+}
+
+// The ops of K register wires of a tile whose wires carry RZ and RY (in
+// either undo order): the RZs of all K wires as one phase, the RYs one wire
+// at a time. M2 m[j][k] is op k of wire j; acc[j * 2 + k] its gradient.
+template <int NV, int K, int C0>
+__device__ __forceinline__ void rzry_ops(float4 (&P)[NV], float4 (&L)[NV], const M2 (*m)[2],
+                                         const float2 (&ph)[8], float *acc) {
+  constexpr int RZ = C0 == kMatDiag ? 0 : 1;   // the RZ's position in undo order
+  if constexpr (RZ == 0) rz_block<NV, K>(P, L, ph, acc, 2);
+  acc[1 - RZ] += reg_op<NV, 0, kMatReal>(P, L, 2, m[0][1 - RZ]);
+  if constexpr (K > 1) acc[2 + 1 - RZ] += reg_op<NV, (K > 1 ? 1 : 0), kMatReal>(P, L, 2, m[1][1 - RZ]);
+  if constexpr (K > 2) acc[4 + 1 - RZ] += reg_op<NV, (K > 2 ? 2 : 0), kMatReal>(P, L, 2, m[2][1 - RZ]);
+  if constexpr (RZ == 1) rz_block<NV, K>(P, L, ph, acc + 1, 2);
 }
 
 // One op on the wire split across a warp pair: the pair trades vectors
@@ -298,12 +377,32 @@ k_adj_warp_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   constexpr int NV = 1 << KH;
   constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + KH);
   constexpr int LANE0 = M * (W0 ? 1 : 0), REG0 = LANE0 + M * NL;
+  // Wires 0..5 and up to two register wires, RZ and RY on every wire (either
+  // undo order): the RZs of all of them go as one phase (rz_wide).
+  constexpr bool kRzRy = M == 2 && W0 && NL == 5 && KH <= 2 &&
+                         ((C0 == kMatDiag && G0 == 3 && C1 == kMatReal && G1 == 2) ||
+                          (C0 == kMatReal && G0 == 2 && C1 == kMatDiag && G1 == 3));
+  constexpr int RZ = C0 == kMatDiag ? 0 : 1;   // the RZ's position in undo order
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t gw = (static_cast<uint64_t>(blockIdx.x) * kThreads + threadIdx.x) >> 5;
   const uint64_t nwarps = static_cast<uint64_t>(gridDim.x) * (kThreads / 32);
   float accf[NOPS];
 #pragma unroll
   for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
+  float sl = 0.0f;   // kRzRy: the lane wires' RZ overlap before its sign
+  const float2 lp = kRzRy ? g.lph[lane] : make_float2(1.0f, 0.0f);
+  // The RY ops of wire 0, the lane wires and the register wires (kRzRy).
+  auto ry_all = [&](float4(&P)[NV], float4(&L)[NV]) {
+    accf[1 - RZ] += wire0_op<NV, kMatReal>(P, L, 2, g.m0[1 - RZ]);
+#pragma unroll
+    for (int k = 0; k < NL; k++)
+      accf[LANE0 + M * k + 1 - RZ] += lane_op_g<NV, kMatReal, 2>(
+          P, L, 1 << g.lbit[k], (lane >> g.lbit[k]) & 1, g.ml[k][1 - RZ]);
+    if constexpr (KH > 0)
+      accf[REG0 + 1 - RZ] += reg_op<NV, 0, kMatReal>(P, L, 2, g.mh[0][1 - RZ]);
+    if constexpr (KH > 1)
+      accf[REG0 + M + 1 - RZ] += reg_op<NV, (KH > 1 ? 1 : 0), kMatReal>(P, L, 2, g.mh[1][1 - RZ]);
+  };
   for (uint64_t ws = gw; ws < nwsites; ws += nwarps) {
     uint64_t b = ws;
 #pragma unroll
@@ -319,13 +418,19 @@ k_adj_warp_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
       P[l] = psi[v];
       L[l] = lam[v];
     }
-    if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
+    if constexpr (kRzRy) {
+      if constexpr (RZ == 1) ry_all(P, L);
+      rz_wide<NV, KH>(P, L, g.ph[0], lp, accf[RZ], sl, accf + REG0 + RZ, M);
+      if constexpr (RZ == 0) ry_all(P, L);
+    } else {
+      if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
 #pragma unroll
-    for (int k = 0; k < NL; k++)
-      lane_ops<M, NV, C0, G0, C1, G1>(P, L, g.lbit[k], lane, g.ml[k], accf + LANE0 + M * k);
-    if constexpr (KH > 0) reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
-    if constexpr (KH > 1) reg_ops<M, NV, (KH > 1 ? 1 : 0), C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
-    if constexpr (KH > 2) reg_ops<M, NV, (KH > 2 ? 2 : 0), C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
+      for (int k = 0; k < NL; k++)
+        lane_ops<M, NV, C0, G0, C1, G1>(P, L, g.lbit[k], lane, g.ml[k], accf + LANE0 + M * k);
+      if constexpr (KH > 0) reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
+      if constexpr (KH > 1) reg_ops<M, NV, (KH > 1 ? 1 : 0), C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
+      if constexpr (KH > 2) reg_ops<M, NV, (KH > 2 ? 2 : 0), C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
+    }
 #pragma unroll
     for (int l = 0; l < NV; l++) {
       uint64_t v = base;
@@ -335,6 +440,11 @@ k_adj_warp_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
       psi[v] = P[l];
       lam[v] = L[l];
     }
+  }
+  if constexpr (kRzRy) {
+#pragma unroll
+    for (int k = 0; k < NL; k++)
+      accf[LANE0 + M * k + RZ] += ((lane >> g.lbit[k]) & 1) ? -sl : sl;
   }
   double acc[NOPS];
 #pragma unroll
@@ -366,6 +476,10 @@ k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsite
   constexpr int SPB = (kThreads / 32) / NW;   // sites per block
   constexpr int ROWS = NV * NW;               // rows of one state in a site
   constexpr int NOPS = M * KH;
+  // RZ and RY on every wire (either undo order): the RZs of a layout's
+  // register wires go as one phase per vector (rzry_ops).
+  constexpr bool kRzRy = M == 2 && ((C0 == kMatDiag && G0 == 3 && C1 == kMatReal && G1 == 2) ||
+                                    (C0 == kMatReal && G0 == 2 && C1 == kMatDiag && G1 == 3));
   static_assert(SPB >= 1 && SPB * NW == kThreads / 32, "whole sites per block");
   extern __shared__ __align__(16) float4 xb[];   // [site][state][row][32 lanes]
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -460,9 +574,13 @@ k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsite
         P[l] = site_p[row_a(l) * 32 + lane];
         L[l] = site_l[row_a(l) * 32 + lane];
       }
-      reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf);
-      reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + M);
-      reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + 2 * M);
+      if constexpr (kRzRy) {
+        rzry_ops<NV, 3, C0>(P, L, g.mh, g.ph[0], accf);
+      } else {
+        reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf);
+        reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + M);
+        reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + 2 * M);
+      }
 #pragma unroll
       for (int l = 0; l < NV; l++) {
         site_p[row_a(l) * 32 + lane] = P[l];
@@ -480,9 +598,13 @@ k_adj_blk_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nsite
     site_sync();   // every warp has read its second layout: the slots are free
     if (active) {
       prefetch(r + 1);
-      reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[3], accf + 3 * M);
-      if constexpr (WB > 1) reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[4], accf + 4 * M);
-      if constexpr (WB > 2) reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[5], accf + 5 * M);
+      if constexpr (kRzRy) {
+        rzry_ops<NV, WB, C0>(P, L, g.mh + 3, g.ph[1], accf + 3 * M);
+      } else {
+        reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[3], accf + 3 * M);
+        if constexpr (WB > 1) reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[4], accf + 4 * M);
+        if constexpr (WB > 2) reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[5], accf + 5 * M);
+      }
       // A warp that gave up a wait leaves the states alone (the host refuses
       // the pass and resets the simulator's state).
       if (!stalled) {
@@ -647,6 +769,49 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
   }
   const bool wide = w0 == 1 && nl == 5, narrow = w0 == 0 && nl == 0;
   if (!wide && !narrow) return 1;
+  // RZ and RY on every wire: each layout's RZ undos of the register wires as
+  // one phase per register vector, multiplied out in double from the
+  // narrowed matrices (one rounding instead of one per wire).
+  if (M == 2 && (seq[0] == kRz) != (seq[1] == kRz)) {
+    const int rz = seq[0] == kRz ? 0 : 1;
+    auto phase = [&](int j0, int cnt, float2(&out)[8]) {
+      for (int l = 0; l < 8; l++) {
+        double re = 1.0, im = 0.0;
+        for (int j = 0; j < cnt; j++) {
+          const float2 e = ((l >> j) & 1) ? u.mh[j0 + j][rz].d : u.mh[j0 + j][rz].a;
+          const double nr = re * e.x - im * e.y, ni = re * e.y + im * e.x;
+          re = nr;
+          im = ni;
+        }
+        out[l] = make_float2(static_cast<float>(re), static_cast<float>(im));
+      }
+    };
+    if (wide) {
+      // ph[0][2 l + b]: the register wires' entries by l times wire 0's by b
+      float2 reg[8];
+      phase(0, std::min(kh, 3), reg);
+      for (int l = 0; l < 4; l++)
+        for (int b = 0; b < 2; b++) {
+          const float2 r = reg[l], e = b ? u.m0[rz].d : u.m0[rz].a;
+          const double re = static_cast<double>(r.x) * e.x - static_cast<double>(r.y) * e.y;
+          const double im = static_cast<double>(r.x) * e.y + static_cast<double>(r.y) * e.x;
+          u.ph[0][2 * l + b] = make_float2(static_cast<float>(re), static_cast<float>(im));
+        }
+      for (int ln = 0; ln < 32; ln++) {
+        double re = 1.0, im = 0.0;
+        for (int k = 0; k < 5; k++) {
+          const float2 e = ((ln >> u.lbit[k]) & 1) ? u.ml[k][rz].d : u.ml[k][rz].a;
+          const double nr = re * e.x - im * e.y, ni = re * e.y + im * e.x;
+          re = nr;
+          im = ni;
+        }
+        u.lph[ln] = make_float2(static_cast<float>(re), static_cast<float>(im));
+      }
+    } else {
+      phase(0, std::min(kh, 3), u.ph[0]);
+      if (kh > 3) phase(3, kh - 3, u.ph[1]);
+    }
+  }
   double *p = out.p;
   if (kh >= 5) {
     if (!narrow) return 1;
