@@ -515,7 +515,9 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
       if (wires[o] >= 6) high[nh++] = wires[o];
     }
   }
-  if (ngrad > 16) return -1;
+  // Sixteen gradients a pass, or twenty in the compile-time tile of wire 0,
+  // wires 1..5 and four wires >= 6 with RZ then RY on every wire.
+  if (ngrad > 20) return -1;
   if ((nh == 5 || nh == 6) && !low && n >= 6 + nh) {
     // Block tile: only the compile-time (uniform) kernels take five or six
     // wires >= 6 in one pass; any other tile of that shape is refused.
@@ -582,10 +584,14 @@ extern "C" int qmk_adjoint_group(float *psi, float *lam, uint32_t n, uint32_t no
     float4 *p4 = reinterpret_cast<float4 *>(psi), *l4 = reinterpret_cast<float4 *>(lam);
     cudaStream_t s = (cudaStream_t)stream;
     const Area a = area_of(ws);
+    if (ngrad > 16) {   // only the compile-time tiles take more
+      const int rc = qmk_adj::launch_uniform(static_cast<int>(nh), p4, l4, nw, g, out, a, s);
+      return rc == 1 ? -1 : rc;
+    }
     const int ng = ngrad == 0 ? 0 : (ngrad <= 4 ? 4 : (ngrad <= 8 ? 8 : 16));
     return qmk_adj::launch_tiles(static_cast<int>(nh), ng, p4, l4, nw, g, out, a, s);
   }
-  if (nd > 3 || n - 1 < nd || nops > kMaxOps) return -1;
+  if (nd > 3 || n - 1 < nd || nops > kMaxOps || ngrad > 16) return -1;
   std::sort(distinct, distinct + nd);
   GroupAdjArgs g{};
   OutSlots<kMaxOps> out{};

@@ -89,12 +89,14 @@ __device__ __forceinline__ void rz_block(float4 (&P)[NV], float4 (&L)[NV], const
 // (the tile of wires 0..5 with an RZ on every wire): wire 0's overlap is
 // q0 - q1 of each vector's two amplitudes, a register wire's +-Q as in
 // rz_block, and a lane wire's the lane's sign times the sum of Q over the
-// thread's vectors (sl; the sign goes on after the last site). One phase per
-// amplitude, lph[lane] ph[2 l + b], undoes them all.
+// thread's vectors (sl; the sign goes on after the last site), as is that of
+// a wire split across a warp pair (by the warp's half). One phase per
+// amplitude, lp ph[2 l + b], undoes them all (lp: the lane wires' product,
+// and the split wire's entry).
 template <int NV, int KH>
-__device__ __forceinline__ void rz_wide(float4 (&P)[NV], float4 (&L)[NV], const float2 (&ph)[8],
+__device__ __forceinline__ void rz_wide(float4 (&P)[NV], float4 (&L)[NV], const float2 *ph,
                                         float2 lp, float &a0, float &sl, float *ar, int stride) {
-  static_assert(NV <= 4, "two register wires at most");
+  static_assert(NV <= 8, "three register wires at most (a table of 2 NV phases)");
   float r[KH > 0 ? KH : 1];
 #pragma unroll
   for (int j = 0; j < KH; j++) r[j] = 0.0f;
@@ -232,6 +234,11 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   constexpr int NOPS = M * ((W0 ? 1 : 0) + NL + 4);
   constexpr int LANE0 = M * (W0 ? 1 : 0), REG0 = LANE0 + M * NL;
   constexpr bool kPipe = M > 1 || W0;
+  // Wires 0..5 and four wires >= 6 with RZ then RY (undo order) on every
+  // wire: the RZs of all ten go as one phase (rz_wide), the split wire's by
+  // the warp's half.
+  constexpr bool kRzRy = M == 2 && W0 && NL == 5 && C0 == kMatDiag && G0 == 3 &&
+                         C1 == kMatReal && G1 == 2;
   extern __shared__ __align__(16) float4 xs[];   // [warp][state][NV][32 lanes]
   const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const uint32_t half = warp & 1;
@@ -244,6 +251,9 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   float accf[NOPS];
 #pragma unroll
   for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
+  float sl = 0.0f;   // kRzRy: the lane and split wires' RZ overlap before its sign
+  const float2 lp = kRzRy ? cmul(g.lph[lane], half ? g.mh[3][0].d : g.mh[3][0].a)
+                          : make_float2(1.0f, 0.0f);
   auto site = [&](uint64_t r) {
     return r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) + (warp >> 1);
   };
@@ -334,18 +344,35 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     // Pipelined: the split wire's ops first. They rewrite all of P and L, so
     // by their end this thread's slot reads are done; the partner's reads of
     // its slots end at the barrier that closes an exchange.
-    if constexpr (kPipe) {
-      split_ops();
+    if constexpr (kRzRy) {
+      // every wire's RZ as one phase, then the split wire's RY (an exchange),
+      // the next round's copies, and the other wires' RYs
+      rz_wide<NV, 3>(P, L, &g.ph[0][0], lp, accf[0], sl, accf + REG0, M);
+      accf[REG0 + 3 * M + 1] += split_one<kMatReal, 2>(P, L, mine_p, mine_l, oth_p, oth_l,
+                                                        half != 0, warp >> 1, g.mh[3][1]);
       prefetch(r + 1);
-    }
-    if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
+      accf[1] += wire0_op<NV, kMatReal>(P, L, 2, g.m0[1]);
 #pragma unroll
-    for (int k = 0; k < NL; k++)
-      lane_ops<M, NV, C0, G0, C1, G1>(P, L, g.lbit[k], lane, g.ml[k], accf + LANE0 + M * k);
-    reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
-    reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
-    reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
-    if constexpr (!kPipe) split_ops();
+      for (int k = 0; k < NL; k++)
+        accf[LANE0 + M * k + 1] += lane_op_g<NV, kMatReal, 2>(
+            P, L, 1 << g.lbit[k], (lane >> g.lbit[k]) & 1, g.ml[k][1]);
+      accf[REG0 + 1] += reg_op<NV, 0, kMatReal>(P, L, 2, g.mh[0][1]);
+      accf[REG0 + M + 1] += reg_op<NV, 1, kMatReal>(P, L, 2, g.mh[1][1]);
+      accf[REG0 + 2 * M + 1] += reg_op<NV, 2, kMatReal>(P, L, 2, g.mh[2][1]);
+    } else {
+      if constexpr (kPipe) {
+        split_ops();
+        prefetch(r + 1);
+      }
+      if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
+#pragma unroll
+      for (int k = 0; k < NL; k++)
+        lane_ops<M, NV, C0, G0, C1, G1>(P, L, g.lbit[k], lane, g.ml[k], accf + LANE0 + M * k);
+      reg_ops<M, NV, 0, C0, G0, C1, G1>(P, L, g.mh[0], accf + REG0);
+      reg_ops<M, NV, 1, C0, G0, C1, G1>(P, L, g.mh[1], accf + REG0 + M);
+      reg_ops<M, NV, 2, C0, G0, C1, G1>(P, L, g.mh[2], accf + REG0 + 2 * M);
+      if constexpr (!kPipe) split_ops();
+    }
     // A warp that gave up a wait computed on slots that may not have held
     // this round's rows: it leaves the states alone (the host refuses the
     // pass and resets the simulator's state).
@@ -361,6 +388,12 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
   if constexpr (kPipe) {
     if (stalled && !__all_sync(0xffffffffu, mbar_wait(&mbar[warp], stalled_parity)) && lane == 0)
       atomicAdd(a.waits, 1u);
+  }
+  if constexpr (kRzRy) {
+#pragma unroll
+    for (int k = 0; k < NL; k++)
+      accf[LANE0 + M * k] += ((lane >> g.lbit[k]) & 1) ? -sl : sl;
+    accf[REG0 + 3 * M] += half ? -sl : sl;
   }
   double acc[NOPS];
 #pragma unroll
@@ -420,7 +453,7 @@ k_adj_warp_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     }
     if constexpr (kRzRy) {
       if constexpr (RZ == 1) ry_all(P, L);
-      rz_wide<NV, KH>(P, L, g.ph[0], lp, accf[RZ], sl, accf + REG0 + RZ, M);
+      rz_wide<NV, KH>(P, L, &g.ph[0][0], lp, accf[RZ], sl, accf + REG0 + RZ, M);
       if constexpr (RZ == 0) ry_all(P, L);
     } else {
       if constexpr (W0) w0_ops<M, NV, C0, G0, C1, G1>(P, L, g.m0, accf);
@@ -787,15 +820,19 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
       }
     };
     if (wide) {
-      // ph[0][2 l + b]: the register wires' entries by l times wire 0's by b
+      // ph[2 l + b] (both rows as one table): the register wires' entries by
+      // l (up to three wires; a fourth is split across a warp pair) times
+      // wire 0's by b
       float2 reg[8];
-      phase(0, std::min(kh, 3), reg);
-      for (int l = 0; l < 4; l++)
+      const int kr = std::min(kh, 3);
+      phase(0, kr, reg);
+      float2 *flat = &u.ph[0][0];
+      for (int l = 0; l < (1 << kr); l++)
         for (int b = 0; b < 2; b++) {
           const float2 r = reg[l], e = b ? u.m0[rz].d : u.m0[rz].a;
           const double re = static_cast<double>(r.x) * e.x - static_cast<double>(r.y) * e.y;
           const double im = static_cast<double>(r.x) * e.y + static_cast<double>(r.y) * e.x;
-          u.ph[0][2 * l + b] = make_float2(static_cast<float>(re), static_cast<float>(im));
+          flat[2 * l + b] = make_float2(static_cast<float>(re), static_cast<float>(im));
         }
       for (int ln = 0; ln < 32; ln++) {
         double re = 1.0, im = 0.0;
@@ -859,6 +896,8 @@ int launch_uniform(int kh, float4 *psi, float4 *lam, uint64_t nw, const WarpAdjA
     QMK_UNI_RX(3)
 #undef QMK_UNI_RX
   }
+  if (M == 2 && seq[0] == kRz && seq[1] == kRy && wide && kh == 4)
+    return launch_pair<true, 5, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);
   if (M == 2 && seq[0] == kRz && seq[1] == kRy && kh <= 3) {
     if (wide && kh == 2)
       return launch_warp<2, true, 5, 2, kMatDiag, 3, kMatReal, 2>(psi, lam, nw, u, p, slots, a, s);

@@ -14,6 +14,11 @@ uint32_t popc(uint64_t x) { return static_cast<uint32_t>(__builtin_popcountll(x)
 constexpr uint32_t kWindowOps = 16;     // ops per window pass below 6 qubits
 constexpr uint32_t kWideWindowOps = 32;  // ops per warp-tile window pass
 constexpr uint32_t kWindowGrads = 16;   // gradients per window pass
+// ... and in the compile-time tile of wire 0, wires 1..5 and four wires >= 6
+// that all carry RZ then RY (undo order): the first tile of a
+// hardware-efficient layer.
+constexpr uint32_t kWideUniformGrads = 20;
+constexpr uint32_t kSigRzRy = 6;          // uniform_signature of RZ then RY
 
 // The structure the kernel layer finds in a 2x2 once narrowed to float (the
 // kMat* classes of kcommon.cuh): 3 diagonal, 1 real, 2 RX-like, 0 general.
@@ -625,7 +630,7 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
         o.slot = static_cast<uint32_t>(k);
         wire_ops[w].push_back(o);
       }
-      if (w >= 6) wire_sig[w] = uniform_signature(wire_ops[w]);
+      wire_sig[w] = uniform_signature(wire_ops[w]);
     }
     // The block tiles of a run of wires sharing one rotation sequence split
     // it evenly: a run of R wires takes ceil(R / tile_high) passes of at most
@@ -652,6 +657,7 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
     // moved to the block tiles costs more than it saves (the 28-qubit HEA
     // gradient 0.108 -> 0.120 s), so there it keeps what fits.
     uint32_t first_high = max_high;
+    bool wide_first = false;
     {
       uint32_t run = 0, sig0 = 0, low_grads = 0, high_grads = 0;
       bool uniform = true, low = false;
@@ -670,6 +676,17 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
         }
         uniform &= wire_sig[w] != 0 && wire_sig[w] == sig0;
         run++;
+      }
+      // The first tile of an RZ-then-RY layer takes four wires >= 6 (twenty
+      // gradients, where sixteen allow two) when that saves a block pass: at
+      // 28 qubits 2 + 5, 5, 5, 5 wires >= 6 become 4 + 6, 6, 6.
+      bool low_rzry = n >= 10;
+      for (uint32_t w = 0; w < 6 && w < n; w++) low_rzry &= wire_sig[w] == kSigRzRy;
+      if (low_rzry && uniform && sig0 == kSigRzRy && run >= 4 && max_high >= 4 &&
+          max_high_blk >= 5) {
+        const uint32_t before = (run - 2 + max_high_blk - 1) / max_high_blk;
+        const uint32_t after = (run - 4 + max_high_blk - 1) / max_high_blk;
+        wide_first = after < before;
       }
       if (low && uniform && run > 0 && max_high_blk >= 5 && high_grads <= 1) {
         // as many as the first tile's gradient slots allow
@@ -710,10 +727,15 @@ std::vector<BackwardStep> backward_schedule(const Circuit &c, uint32_t tile_high
         // block tiles: five or six wires >= 6 of one rotation sequence.
         const bool blk = !tile_low && w >= 6 && sig != 0 && (tile.empty() || sig == tile_sig);
         if (blk && tile.empty()) blk_cap = balanced_cap(w);
+        // A tile of wire 0 and wires 1..5 that all carry RZ then RY takes four
+        // wires >= 6 with the same ops (twenty gradients) where that saves a pass.
+        const bool wide_rzry = wide_first && tile_low && others == 5 + highs &&
+                               tile.size() == 12 + 2 * highs && tile_sig == kSigRzRy &&
+                               sig == kSigRzRy;
         full = tile.size() + ops.size() > max_ops ||
                highs + need_high >
                    (blk ? std::max(blk_cap, max_high) : (tile_low ? first_high : max_high)) ||
-               grads + wgrads > kWindowGrads;
+               grads + wgrads > (wide_rzry ? kWideUniformGrads : kWindowGrads);
         if (!full && !blk && highs > max_high) full = true;   // a block tile takes no other wire
       } else {
         const uint32_t cap = (others + need_other >= 3) ? 8u : 16u;

@@ -333,7 +333,16 @@ def replay_backward(n, gates, terms, tile_high):
                     assert seq in {("rx",), ("ry",), ("rz",), ("rz", "ry"), ("ry", "rz")}, seq
             else:
                 assert len(ops) <= 16
-            assert sum(g != 0 for _, _, g, _ in ops) <= 16
+            ngrad = sum(g != 0 for _, _, g, _ in ops)
+            if ngrad > 16:
+                # only the compile-time first tile of an RZ-then-RY layer:
+                # wire 0, wires 1..5 and four wires >= 6, each with RZ then
+                # RY (undo order), twenty gradients
+                assert ngrad <= 20 and set(range(6)) <= wires
+                assert len({w for w in wires if w >= 6}) == 4
+                for w in wires:
+                    seq = tuple(rotation_kind(m, g) for ww, m, g, _ in ops if ww == w)
+                    assert seq == ("rz", "ry"), seq
             for w, minv, gen, slot in ops:
                 if gen:
                     pl = apply_1q(psi, n, w, PAULI[gen])
@@ -637,3 +646,26 @@ def test_random_circuits_replay_property():
         assert np.abs(lam - h_apply(oracle.run(n, gates), n, terms)).max() < 1e-12
 
     check()
+
+
+@pytest.mark.parametrize("n,first,blocks", [(20, 2, [6, 6]), (22, 4, [6, 6]), (28, 4, [6, 6, 6]),
+                                            (33, 4, [6, 6, 6, 5])])
+def test_wide_first_tile_of_rzry_layers(n, first, blocks):
+    """An HEA layer's first tile (wire 0, wires 1..5) takes four wires >= 6
+    with their twenty gradients only where that saves a block pass (at 20
+    qubits two and then 6 + 6 either way)."""
+    gates, _ = W.hea_gradient_problem(n, depth=1, seed=5)
+    steps = decode_backward(W.to_circuit(n, gates).schedule_export("backward", tile_high=6))
+    shape = [len({w for w, _, _, _ in s[1] if w >= 6}) for s in steps if s[0] == "window"]
+    assert shape == [first] + blocks, shape
+
+
+def test_wide_first_tile_gradient_replay():
+    n = 22
+    gates, terms = W.hea_gradient_problem(n, depth=1, seed=7)
+    grad, touched, steps = replay_backward(n, gates, terms, 6)
+    assert max(sum(g != 0 for _, _, g, _ in s[1]) for s in steps if s[0] == "window") == 20
+    _, want = oracle.energy_and_gradient(n, gates, terms)
+    assert np.abs(grad - want).max() < 1e-10
+    params = np.array([len(g[2]) > 0 for g in gates])
+    assert (touched == params).all()
