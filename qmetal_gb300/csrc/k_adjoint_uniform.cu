@@ -252,8 +252,6 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
 #pragma unroll
   for (int t = 0; t < NOPS; t++) accf[t] = 0.0f;
   float sl = 0.0f;   // kRzRy: the lane and split wires' RZ overlap before its sign
-  const float2 lp = kRzRy ? cmul(g.lph[lane], half ? g.mh[3][0].d : g.mh[3][0].a)
-                          : make_float2(1.0f, 0.0f);
   auto site = [&](uint64_t r) {
     return r * per_round + static_cast<uint64_t>(blockIdx.x) * (kThreads / 64) + (warp >> 1);
   };
@@ -347,7 +345,12 @@ k_adj_pair_uni(float4 *__restrict__ psi, float4 *__restrict__ lam, uint64_t nwsi
     if constexpr (kRzRy) {
       // every wire's RZ as one phase, then the split wire's RY (an exchange),
       // the next round's copies, and the other wires' RYs
-      rz_wide<NV, 3>(P, L, &g.ph[0][0], lp, accf[0], sl, accf + REG0, M);
+      {
+        // the lane wires' phase and the split wire's, formed each round (kept
+        // across the loop it pushed the tile into spills)
+        const float2 lp = cmul(g.lph[lane], half ? g.mh[3][0].d : g.mh[3][0].a);
+        rz_wide<NV, 3>(P, L, &g.ph[0][0], lp, accf[0], sl, accf + REG0, M);
+      }
       accf[REG0 + 3 * M + 1] += split_one<kMatReal, 2>(P, L, mine_p, mine_l, oth_p, oth_l,
                                                         half != 0, warp >> 1, g.mh[3][1]);
       prefetch(r + 1);
