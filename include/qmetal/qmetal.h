@@ -164,7 +164,7 @@ size_t qm_circuit_plan_export(qm_circuit c, int collapse_1q_windows,
  * needed), in a flat double layout:
  *   which = 0: the merged forward pass of the default plan (qm_run_merged);
  *   which = 1: the block-wise backward sweep (qm_energy_and_gradient) with
- *              `tile_high` wires >= 6 per window pass (1..4);
+ *              `tile_high` wires >= 6 per window pass (1..6);
  *   which = 2: the co-state lambda = H psi of `h` for the circuit's width.
  * Forward steps: 0 group (nw, then wire and a row-major 2x2 as re/im pairs per
  * wire), 1 gather (n, cols[n], off, nops, plan op indices), 2 plan op (index).
@@ -174,7 +174,8 @@ size_t qm_circuit_plan_export(qm_circuit c, int collapse_1q_windows,
  * ngates, gate indices), 3 gate undo (index). Co-state steps: 0 Z strings
  * (nt, (z mask, coeff) x nt), 1 one-wire flips (overwrite, nt, (wire, sign
  * mask, Y count, coeff) x nt), 2 one flip mask (overwrite, flip, nt, (sign
- * mask, Y count, coeff) x nt), 3 zero, 4 energy. A gather step computes
+ * mask, Y count, coeff) x nt), 3 zero, 4 energy, 5 transverse field
+ * (overwrite, energy 0/1/2, nw, (wire, coeff) x nw). A gather step computes
  * dst[y] = src[off ^ XOR of cols[j] over the set bits j of y].
  * Writes at most `cap` doubles; returns the full length, or 0 on error. */
 size_t qm_schedule_export(qm_circuit c, const qm_hamiltonian *h, int which,
