@@ -201,11 +201,12 @@ int qmk_adjoint_diagonal(float *psi, float *lambda, uint32_t n, uint32_t num_ter
  * Im<lambda|P|psi> if gens[o] is 1/2/3 (X/Y/Z), then applies
  * minv[8o..8o+7] to both states; one pass. From n >= 6 + h a tile holds wire
  * 0, any of wires 1..5 and h <= 4 wires >= 6, up to 32 ops of which up to 16
- * carry a gradient; below that, wire 0 and up to three wires >= 1 and 16
- * ops. A tile of five or six wires >= 6 and no other wire is taken when
- * every wire carries the same rotation sequence (one RX, RY or RZ per wire,
- * or RZ then RY, or RY then RZ). Returns -1 (nothing launched) for any other
- * shape. Replaces the
+ * carry a gradient (20 in the tile of wire 0, wires 1..5 and four wires >= 6
+ * where every wire carries RZ then RY); below that, wire 0 and up to three
+ * wires >= 1 and 16 ops. A tile of five or six wires >= 6 and no other wire
+ * is taken when every wire carries the same rotation sequence (one RX, RY or
+ * RZ per wire, or RZ then RY, or RY then RZ). Returns -1 (nothing launched)
+ * for any other shape. Replaces the
  * per-gate reduce_pauli2 and undo dispatches (kernels.metal:331-360;
  * simulator.mm:914-959). */
 int qmk_adjoint_group(float *psi, float *lambda, uint32_t n, uint32_t num_ops,
