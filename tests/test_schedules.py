@@ -669,3 +669,52 @@ def test_wide_first_tile_gradient_replay():
     assert np.abs(grad - want).max() < 1e-10
     params = np.array([len(g[2]) > 0 for g in gates])
     assert (touched == params).all()
+
+
+def test_wide_layers_and_fields_property():
+    """Property test at 10..16 qubits, where the transverse-field co-state
+    passes and (from 15 qubits) the twenty-gradient first tile of
+    RZ-then-RY layers apply:
+    random RY+RZ layers (on every wire or on a random subset) between CX
+    ladders, and Hamiltonians of a ZZ ring, plain X fields on random wires
+    (repeats summed) and sometimes other terms. The co-state replay gives
+    H psi and the energy the passes carry; the backward replay gives the
+    oracle's gradient."""
+    hyp = pytest.importorskip("hypothesis")
+    st = hyp.strategies
+
+    @hyp.settings(max_examples=40, deadline=None, derandomize=True)
+    @hyp.given(st.data())
+    def check(data):
+        n = data.draw(st.integers(10, 16))
+        layers = data.draw(st.integers(1, 2))
+        ang = st.floats(-3.0, 3.0, allow_nan=False)
+        # (the ladder closes the Hadamard layer's window, so that each RY+RZ
+        # layer is a window of its own)
+        gates = [(H, (q,), ()) for q in range(n)] + [(CX, (q, q + 1), ()) for q in range(n - 1)]
+        for _ in range(layers):
+            full = data.draw(st.booleans())
+            wires = list(range(n)) if full else sorted(
+                data.draw(st.sets(st.integers(0, n - 1), min_size=1, max_size=n)))
+            for q in wires:
+                gates += [(RY, (q,), (data.draw(ang),)), (RZ, (q,), (data.draw(ang),))]
+            gates += [(CX, (q, q + 1), ()) for q in range(n - 1)]
+        field = data.draw(st.lists(st.integers(0, n - 1), min_size=1, max_size=2 * n))
+        terms = [(-1.0, 0, 0, (1 << i) | (1 << ((i + 1) % n))) for i in range(n)]
+        terms += [(data.draw(ang) / 3.0, 1 << w, 0, 0) for w in field]
+        if data.draw(st.booleans()):
+            terms += random_terms(n, 3, data.draw(st.integers(0, 2**31 - 1)))
+        psi = oracle.run(n, gates)
+        lam, covered, energy = replay_costate(n, psi, terms)
+        want = h_apply(psi, n, terms)
+        assert np.abs(lam - want).max() < 1e-12
+        assert abs(energy - float(np.vdot(psi, want).real)) < 1e-12
+        assert_covers(covered, terms)
+        tile_high = data.draw(st.sampled_from([4, 5, 6]))
+        grad, touched, _ = replay_backward(n, gates, terms, tile_high)
+        _, g0 = oracle.energy_and_gradient(n, gates, terms)
+        assert np.abs(grad - g0).max() < 1e-10
+        params = np.array([len(g[2]) > 0 for g in gates])
+        assert (touched == params).all()
+
+    check()
