@@ -673,13 +673,12 @@ def test_wide_first_tile_gradient_replay():
 
 def test_wide_layers_and_fields_property():
     """Property test at 10..16 qubits, where the transverse-field co-state
-    passes and (from 15 qubits) the twenty-gradient first tile of
-    RZ-then-RY layers apply:
-    random RY+RZ layers (on every wire or on a random subset) between CX
-    ladders, and Hamiltonians of a ZZ ring, plain X fields on random wires
-    (repeats summed) and sometimes other terms. The co-state replay gives
-    H psi and the energy the passes carry; the backward replay gives the
-    oracle's gradient."""
+    passes apply: random RY+RZ layers (on every wire or on a random subset)
+    between CX ladders, and Hamiltonians of a ZZ ring, plain X fields on
+    random wires (repeats summed) and sometimes other terms. The co-state
+    replay gives H psi and the energy the passes carry; the backward replay
+    gives the oracle's gradient. (The twenty-gradient first tile, which pays
+    from 15 qubits, is pinned by the two tests above.)"""
     hyp = pytest.importorskip("hypothesis")
     st = hyp.strategies
 
